@@ -1,0 +1,93 @@
+/*
+ * CPU oracle for the lattice Boltzmann step -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of lettuce's torch step (stream by periodic roll,
+ * masked collide substeps, boundary operators), used by the test-suite as
+ * the checker and by bench.py as the timed CPU baseline. Nothing in the
+ * product (lettuce_gb300/) links, loads or calls it.
+ *
+ * Each routine cites the lettuce source it restates (paths are relative to
+ * the lettuce project root):
+ *   stream          lettuce/_simulation.py:241-256
+ *   masked collide  lettuce/_simulation.py:258-305
+ *   strategies      lettuce/_simulation.py:148-166
+ *   moments         lettuce/_flow.py:157-193
+ *   equilibrium     lettuce/ext/_equilibrium/quadratic_equilibrium.py:11-24
+ *   BGK             lettuce/ext/_collision/bgk_collision.py:17-22
+ *   TRT             lettuce/ext/_collision/trt_collision.py:16-27
+ *   KBC             lettuce/ext/_collision/kbc_collision.py:22-160
+ *   bounce-back     lettuce/ext/_boundary/bounce_back_boundary.py:17-18
+ *   equilibrium BC  lettuce/ext/_boundary/equilibrium_boundary_pu.py:79-84
+ *   anti-bounce-back outlet
+ *                   lettuce/ext/_boundary/anti_bounce_back_outlet.py:71-91
+ *
+ * Parity of this restatement with lettuce itself is pinned by golden
+ * vectors generated from lettuce (tests/golden/make_golden.py).
+ */
+#ifndef LBM_ORACLE_H
+#define LBM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* stencil ids (same numbering as the CUDA library) */
+enum { ORC_D1Q3 = 1, ORC_D2Q9 = 2, ORC_D3Q15 = 3, ORC_D3Q19 = 4, ORC_D3Q27 = 5 };
+/* collision kinds */
+enum { ORC_NO_COLLISION = 0, ORC_BGK = 1, ORC_TRT = 2, ORC_KBC = 3 };
+/* substep kinds */
+enum { ORC_SUB_COLLISION = 0, ORC_SUB_BOUNCE_BACK = 1, ORC_SUB_EQUILIBRIUM_PU = 2,
+       ORC_SUB_ANTI_BOUNCE_BACK = 3, ORC_SUB_NONE = 4 };
+/* streaming strategies: lettuce's StreamingStrategy enum values
+ * (lettuce/cuda_native/_default_code_gen.py:13-17) */
+enum { ORC_NO_STREAMING = 0, ORC_POST_STREAMING = 1, ORC_PRE_STREAMING = 2,
+       ORC_DOUBLE_STREAMING = 3 };
+
+typedef struct {
+    int32_t kind;
+    /* equilibrium BC: density (lattice units) and velocity (lattice units),
+     * broadcast over the grid by element strides (0 = broadcast dim).
+     * strides are given per lettuce dimension (x, y, z order). */
+    const void *rho;
+    const void *u;
+    int64_t rho_stride[3];
+    int64_t u_stride[4]; /* [component, x, y, z] */
+    /* anti-bounce-back: lettuce dimension index of the normal and its sign */
+    int32_t axis;
+    int32_t sign;
+} orc_substep;
+
+typedef struct {
+    int32_t stencil;
+    int32_t res[3];          /* lettuce resolution; unused trailing dims = 1 */
+    int32_t collision;
+    int32_t strategy;
+    double tau;
+    double tau_minus;
+    const uint8_t *ncm;      /* [N] substep index per cell, or NULL */
+    const uint8_t *nsm;      /* [Q][N] no-streaming values, or NULL */
+    int32_t n_sub;
+    int32_t collision_index;
+    const orc_substep *sub;  /* [n_sub] */
+} orc_problem;
+
+int orc_stencil_dq(int stencil, int *d, int *q);
+
+/* nsteps full steps in place on f ([Q][N], lettuce layout); work is a
+ * [Q][N] scratch buffer. Returns 0 on success. */
+int orc_run_f64(const orc_problem *p, double *f, double *work, int nsteps, int nthreads);
+int orc_run_f32(const orc_problem *p, float *f, float *work, int nsteps, int nthreads);
+
+/* density [N] and velocity [D][N] of f */
+int orc_moments_f64(int stencil, const int32_t *res, const double *f, double *rho, double *u, int nthreads);
+int orc_moments_f32(int stencil, const int32_t *res, const float *f, float *rho, float *u, int nthreads);
+
+/* quadratic equilibrium of rho [N], u [D][N] into feq [Q][N] */
+int orc_equilibrium_f64(int stencil, const int32_t *res, const double *rho, const double *u, double *feq, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,318 @@
+"""Generate golden vectors from lettuce itself (its CPU torch path, float64).
+
+Run in a container where the lettuce sources are available:
+
+    PYTHONDONTWRITEBYTECODE=1 \
+    PYTHONPATH=tests/golden/_stubs:/root/reference \
+        python tests/golden/make_golden.py
+
+``_stubs/`` holds empty stand-ins for lettuce's optional imports (mmh3,
+h5py, pyevtk, matplotlib) -- none of them is on the arithmetic path. The
+outputs (``*.npz`` next to this script) are what the CPU oracle and the CUDA
+path are checked against; lettuce itself never runs in the test-suite.
+"""
+import json
+import os
+import sys
+import warnings
+
+import numpy as np
+import torch
+
+warnings.filterwarnings("ignore")
+import lettuce as lt  # noqa: E402
+from lettuce import (Context, Simulation, StreamingStrategy,  # noqa: E402
+                     UnitConversion)
+from lettuce.ext import (D1Q3, D2Q9, D3Q15, D3Q19, D3Q27,  # noqa: E402
+                         AntiBounceBackOutlet, BGKCollision,
+                         BounceBackBoundary, EquilibriumBoundaryPU, ExtFlow,
+                         IncompressibleKineticEnergy, KBCCollision,
+                         MaximumVelocity, NoCollision, Obstacle,
+                         TaylorGreenVortex, TRTCollision, Enstrophy)
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+CTX = Context(device="cpu", dtype=torch.float64, use_native=False)
+STRATS = {"PRE_STREAMING": StreamingStrategy.PRE_STREAMING,
+          "POST_STREAMING": StreamingStrategy.POST_STREAMING}
+
+
+def npf(t):
+    return t.detach().cpu().numpy().copy()
+
+
+class GivenFlow(ExtFlow):
+    """A flow whose populations are given directly (like the DummyFlow of
+    lettuce's tests/conftest.py)."""
+    f_init = None
+    bnds = []
+
+    def __init__(self, stencil, f0, boundaries=()):
+        GivenFlow.f_init = f0
+        self.bnds = list(boundaries)
+        ExtFlow.__init__(self, CTX, list(f0.shape[1:]), 100.0, 0.05,
+                         stencil=stencil)
+
+    def make_resolution(self, resolution, stencil=None):
+        return list(resolution)
+
+    def make_units(self, reynolds_number, mach_number, resolution):
+        return UnitConversion(reynolds_number=reynolds_number,
+                              mach_number=mach_number)
+
+    def initial_pu(self):
+        ...
+
+    def initialize(self):
+        self.f = torch.tensor(GivenFlow.f_init, dtype=torch.float64)
+
+    @property
+    def post_boundaries(self):
+        return self.bnds
+
+
+def collision_of(kind, tau):
+    if kind == "bgk":
+        return BGKCollision(tau=tau)
+    if kind == "trt":
+        return TRTCollision(tau=tau, tau_minus=1.0)
+    if kind == "kbc":
+        return KBCCollision(tau=tau)
+    return NoCollision()
+
+
+def case_tgv(name, stencil, res, re, coll, steps):
+    out = {}
+    for sname, strat in STRATS.items():
+        flow = TaylorGreenVortex(CTX, resolution=res, reynolds_number=re,
+                                 mach_number=0.05, stencil=stencil)
+        f0 = npf(flow.f)
+        tau = flow.units.relaxation_parameter_lu
+        sim = Simulation(flow, collision_of(coll, tau), [],
+                         streaming_strategy=strat)
+        sim(steps)
+        out["f0"] = f0
+        out[f"f_{sname}"] = npf(flow.f)
+        out["tau"] = np.float64(tau)
+    out["steps"] = np.int64(steps)
+    out["meta"] = json.dumps({"flow": "TaylorGreenVortex", "res": res,
+                              "re": re, "ma": 0.05, "collision": coll,
+                              "stencil": stencil.__name__})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_random(name, stencil, res, coll, steps, seed):
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.2 * rng.standard_normal([st.q] + res))
+    tau = 0.73
+    out = {"f0": f0, "tau": np.float64(tau), "steps": np.int64(steps)}
+    for sname, strat in STRATS.items():
+        flow = GivenFlow(st, f0)
+        sim = Simulation(flow, collision_of(coll, tau), [],
+                         streaming_strategy=strat)
+        sim(steps)
+        out[f"f_{sname}"] = npf(flow.f)
+        if coll == "kbc":
+            # KBCCollision relaxes with flow.units.relaxation_parameter_lu,
+            # not with its constructor argument (kbc_collision.py:97-99)
+            out["tau"] = np.float64(flow.units.relaxation_parameter_lu)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res,
+                              "collision": coll})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_obstacle(name, stencil, res, radius, coll, steps):
+    out = {}
+    for sname, strat in STRATS.items():
+        flow = Obstacle(CTX, resolution=res, reynolds_number=100,
+                        mach_number=0.1, domain_length_x=res[0] / 4.0,
+                        stencil=stencil)
+        grid = np.meshgrid(*[np.arange(n) for n in res], indexing="ij")
+        centre = [res[0] / 3.0] + [n / 2.0 - 0.5 for n in res[1:]]
+        r2 = sum((g - c) ** 2 for g, c in zip(grid, centre))
+        mask = r2 < radius ** 2
+        flow.mask = mask
+        flow.initialize()
+        f0 = npf(flow.f)
+        tau = flow.units.relaxation_parameter_lu
+        sim = Simulation(flow, collision_of(coll, tau), [],
+                         streaming_strategy=strat)
+        out["ncm"] = npf(sim.no_collision_mask).astype(np.uint8)
+        out["nsm"] = npf(sim.no_streaming_mask).astype(np.uint8)
+        sim(steps)
+        out["f0"] = f0
+        out["mask"] = mask
+        out[f"f_{sname}"] = npf(flow.f)
+        out["tau"] = np.float64(tau)
+        inlet = flow.post_boundaries[0]
+        out["inlet_u_lu"] = npf(flow.units.convert_velocity_to_lu(
+            inlet.velocity))
+        out["inlet_rho_lu"] = npf(flow.units.convert_pressure_pu_to_density_lu(
+            inlet.pressure))
+    out["steps"] = np.int64(steps)
+    out["meta"] = json.dumps({"flow": "Obstacle", "res": res,
+                              "radius": radius, "collision": coll,
+                              "stencil": stencil.__name__, "re": 100,
+                              "ma": 0.1, "domain_length_x": res[0] / 4.0})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_eqpu_field(name):
+    """equilibrium boundary with a per-cell velocity field and a scalar
+    pressure (lettuce tests/boundary/test_equilibrium_bc_pu.py style)"""
+    st = D2Q9()
+    res = [12, 10]
+    rng = np.random.default_rng(7)
+    w = np.array(st.w).reshape([-1, 1, 1])
+    f0 = w * (1.0 + 0.1 * rng.standard_normal([st.q] + res))
+    mask = np.zeros(res, dtype=bool)
+    mask[3:6, 2:8] = True
+    vel = 0.1 * rng.standard_normal([2] + res)
+    out = {"f0": f0, "mask": mask, "velocity_pu": vel, "pressure_pu": 0.02}
+    for sname, strat in STRATS.items():
+        flow = GivenFlow(st, f0)
+        b = EquilibriumBoundaryPU(CTX, flow, torch.tensor(mask),
+                                  torch.tensor(vel), 0.02)
+        flow.bnds = [b]
+        sim = Simulation(flow, BGKCollision(tau=0.8), [],
+                         streaming_strategy=strat)
+        out["u_lu"] = npf(flow.units.convert_velocity_to_lu(b.velocity))
+        out["rho_lu"] = npf(flow.units.convert_pressure_pu_to_density_lu(
+            b.pressure))
+        sim(3)
+        out[f"f_{sname}"] = npf(flow.f)
+    out["tau"] = np.float64(0.8)
+    out["steps"] = np.int64(3)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_native_kats():
+    """known-answer cases of lettuce's tests/native/test_native_streaming.py
+    (impulse per direction) and test_native_bounce_back.py"""
+    st = D2Q9()
+    f0 = np.zeros([9, 16, 16])
+    for i in range(9):
+        f0[i, i + 1, i + 1] = float(i + 1)
+    flow = GivenFlow(st, f0)
+    Simulation(flow, NoCollision(), [])(1)
+    out = {"stream_f0": f0, "stream_f1": npf(flow.f)}
+    f0 = np.zeros([9, 16, 16])
+    f0[:, 1, 1] = 1.0
+    mask = np.zeros([16, 16], dtype=bool)
+    mask[0, :] = True
+    mask[:, 0] = True
+    mask[2:, :] = True
+    mask[:, 2:] = True
+    flow = GivenFlow(st, f0, [BounceBackBoundary(torch.tensor(mask))])
+    Simulation(flow, NoCollision(), [])(1)
+    out.update({"bb_f0": f0, "bb_mask": mask, "bb_f1": npf(flow.f)})
+    flow = GivenFlow(st, f0, [BounceBackBoundary(torch.tensor(mask))])
+    Simulation(flow, NoCollision(), [])(2)
+    out["bb_f2"] = npf(flow.f)
+    np.savez_compressed(os.path.join(OUT, "native_kats.npz"), **out)
+
+
+def case_observables():
+    out = {}
+    for tag, stencil, res in [("2d", D2Q9, 16), ("3d", D3Q19, 8)]:
+        flow = TaylorGreenVortex(CTX, resolution=res, reynolds_number=1000,
+                                 mach_number=0.05, stencil=stencil)
+        out[f"{tag}_f"] = npf(flow.f)
+        out[f"{tag}_energy"] = np.float64(
+            IncompressibleKineticEnergy(flow)().item())
+        out[f"{tag}_umax"] = np.float64(MaximumVelocity(flow)().item())
+        out[f"{tag}_enstrophy"] = np.float64(Enstrophy(flow)().item())
+        out[f"{tag}_rho"] = npf(flow.rho())
+        out[f"{tag}_u"] = npf(flow.u())
+        out[f"{tag}_units"] = json.dumps({
+            "relaxation_parameter_lu": flow.units.relaxation_parameter_lu,
+            "viscosity_lu": flow.units.viscosity_lu,
+            "characteristic_velocity_lu":
+                flow.units.characteristic_velocity_lu,
+            "characteristic_length_lu": flow.units.characteristic_length_lu,
+            "time_pu_100": flow.units.convert_time_to_pu(100)})
+    np.savez_compressed(os.path.join(OUT, "observables.npz"), **out)
+
+
+def case_tgv_energy_decay():
+    """the 2-D Taylor-Green energy decay: D2Q9 BGK 256^2, Re 1000, Ma 0.05,
+    float64, 1000 steps (POST_STREAMING, lettuce's default)"""
+    flow = TaylorGreenVortex(CTX, resolution=256, reynolds_number=1000,
+                             mach_number=0.05, stencil=D2Q9)
+    energy = IncompressibleKineticEnergy(flow)
+    sim = Simulation(flow, BGKCollision(flow.units.relaxation_parameter_lu),
+                     [])
+    e = [energy().item()]
+    t = [0.0]
+    for _ in range(10):
+        sim(100)
+        e.append(energy().item())
+        t.append(flow.units.convert_time_to_pu(flow.i))
+    nu = flow.units.viscosity_pu
+    out = {"energy": np.array(e), "time_pu": np.array(t),
+           "analytic_ratio": np.exp(-4 * nu * np.array(t)),
+           "u_final": npf(flow.u()).astype(np.float32)}
+    np.savez_compressed(os.path.join(OUT, "tgv2d_energy_256.npz"), **out)
+
+
+def case_adjoint():
+    """gradient of MSE(u(T), target) w.r.t. the initial velocity through
+    lettuce's torch step (torch autograd, float64) -- D2Q9 BGK 32^2,
+    PRE_STREAMING, 10 steps, f0 = feq(rho=1, u0)"""
+    n, steps, tau = 32, 10, 0.56
+    st = D2Q9()
+    gen = torch.Generator().manual_seed(0)
+    x = torch.arange(n, dtype=torch.float64) * 2 * np.pi / n
+    X, Y = torch.meshgrid(x, x, indexing="ij")
+    ulu = 0.05 / np.sqrt(3)
+    u0 = torch.stack([torch.cos(X) * torch.sin(Y),
+                      -torch.sin(X) * torch.cos(Y)]) * ulu
+    u0 = u0 + 1e-3 * torch.randn(u0.shape, generator=gen, dtype=torch.float64)
+    gen1 = torch.Generator().manual_seed(1)
+    target = ulu * torch.randn(u0.shape, generator=gen1, dtype=torch.float64)
+    u0 = u0.clone().requires_grad_(True)
+    flow = GivenFlow(st, np.zeros([9, n, n]))
+    rho0 = torch.ones([1, n, n], dtype=torch.float64)
+    flow.f = flow.equilibrium(flow, rho=rho0, u=u0)
+    sim = Simulation(flow, BGKCollision(tau=tau), [],
+                     streaming_strategy=StreamingStrategy.PRE_STREAMING)
+    sim(steps)
+    loss = torch.mean((flow.u() - target) ** 2)
+    loss.backward()
+    out = {"u0": npf(u0), "target": npf(target), "loss": np.float64(loss.item()),
+           "grad_u0": npf(u0.grad), "tau": np.float64(tau),
+           "steps": np.int64(steps)}
+    np.savez_compressed(os.path.join(OUT, "adjoint_d2q9_32.npz"), **out)
+
+
+def main():
+    torch.set_num_threads(os.cpu_count() or 1)
+    case_tgv("tgv2d_d2q9_bgk", D2Q9, 16, 1000, "bgk", 5)
+    case_tgv("tgv2d_d2q9_trt", D2Q9, [16, 12], 300, "trt", 5)
+    case_tgv("tgv2d_d2q9_kbc", D2Q9, 16, 1000, "kbc", 5)
+    case_tgv("tgv3d_d3q19_bgk", D3Q19, 8, 1600, "bgk", 3)
+    case_tgv("tgv3d_d3q27_kbc", D3Q27, 8, 1600, "kbc", 3)
+    seed = 0
+    for stencil, res in [(D1Q3, [13]), (D2Q9, [7, 5]), (D3Q15, [5, 4, 3]),
+                         (D3Q19, [5, 4, 3]), (D3Q27, [5, 4, 3])]:
+        colls = ["bgk", "trt", "none"]
+        if stencil in (D2Q9, D3Q27):
+            colls.append("kbc")
+        for coll in colls:
+            case_random(f"random_{stencil.__name__.lower()}_{coll}", stencil,
+                        res, coll, 2, seed)
+            seed += 1
+    case_obstacle("obstacle2d_d2q9_bgk", D2Q9, [32, 16], 3.0, "bgk", 10)
+    case_obstacle("obstacle3d_d3q27_kbc", D3Q27, [24, 8, 8], 2.0, "kbc", 3)
+    case_eqpu_field("eqpu_field_d2q9")
+    case_native_kats()
+    case_observables()
+    case_adjoint()
+    if "--no-energy" not in sys.argv:
+        case_tgv_energy_decay()
+    print("golden vectors written to", OUT)
+
+
+if __name__ == "__main__":
+    main()
