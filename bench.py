@@ -1,0 +1,410 @@
+"""Benchmark of the lattice Boltzmann step on GB300.
+
+Workload (one "step" = one LBM time step over the whole grid): D3Q19 BGK
+3-D Taylor-Green vortex, 256^3 periodic, Re 1600, Ma 0.05, stream+collide in
+one pull-pattern pass (lettuce PRE_STREAMING, the CLI benchmark default).
+Populations stored as float32 (headline ``value``) and as shifted float16
+with float32 arithmetic (``fp16_shifted``); the in-place AA variants are
+reported beside them. The 16-bit run's velocity error against a float64 run
+of the same 1000 steps is measured in ``accuracy``.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the CPU oracle (a C restatement of lettuce's torch
+step) on this host's cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "D3Q19 MLUPS and % HBM peak, FP32 vs FP16-store at stated FP64 error"
+UNIT = "MLUPS"
+RES = [256, 256, 256]
+RE, MA = 1600, 0.05
+Q = 19
+BYTES_PER_CELL = {"f32": 2 * Q * 4, "f16": 2 * Q * 2}  # read Q + write Q populations
+WORKLOAD = "D3Q19 BGK Taylor-Green 256^3 periodic, Re 1600, Ma 0.05"
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel_key):
+    """DRAM bytes per launch from the committed ncu summary, if present"""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(kernel_key)
+    except (OSError, ValueError):
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs"""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            lines = open(self.path).read().strip().splitlines()
+        except OSError:
+            lines = []
+        for ln in lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if self.path:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": smax or None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if (args.impl == "ours" and torch.cuda.is_available()) else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_mlups(res, steps_budget_s, nthreads, steps_cap=None):
+    """float32 oracle (C port of lettuce's step) on a TGV field: returns
+    (MLUPS, steps run, cells per step, seconds)"""
+    from oracle import oracle as orc
+    orc.build()
+    import lettuce_gb300 as lt
+    import torch
+    ctx = lt.Context("cpu", torch.float32)
+    flow = lt.TaylorGreenVortex(ctx, list(res), RE, MA, lt.D3Q19)
+    f = flow.f.numpy()
+    tau = flow.units.relaxation_parameter_lu
+    n = int(np.prod(res))
+    t0 = time.perf_counter()
+    f = orc.run("D3Q19", f, 1, collision="bgk", tau=tau, strategy="PRE_STREAMING",
+                nthreads=nthreads)
+    t1 = time.perf_counter() - t0
+    steps = max(1, int(steps_budget_s / max(t1, 1e-6)))
+    if steps_cap is not None:
+        steps = min(steps, steps_cap)
+    t0 = time.perf_counter()
+    orc.run("D3Q19", f, steps, collision="bgk", tau=tau, strategy="PRE_STREAMING",
+            nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return steps * n / dt / 1e6, steps, n, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    # bounded sample: the full 256^3 grid if K steps fit the budget, else a
+    # periodic 256 x 256 x Z crop with the same per-cell work
+    budget = float(os.environ.get("LGB_REF_BUDGET_S", "60"))
+    from oracle import oracle as orc
+    orc.build()
+    res = list(RES)
+    probe, _, _, dt1 = oracle_mlups([64, 64, 64], 0.0, nthreads, steps_cap=1)
+    est_step = (np.prod(RES) / 1e6) / max(probe, 1e-6)
+    total = est_step * (args.steps + args.warmup)
+    if total > budget:
+        z = max(8, int(RES[2] * budget / total) // 8 * 8)
+        res = [RES[0], RES[1], z]
+    import lettuce_gb300 as lt
+    import torch
+    ctx = lt.Context("cpu", torch.float32)
+    flow = lt.TaylorGreenVortex(ctx, res, RE, MA, lt.D3Q19)
+    f = flow.f.numpy()
+    tau = flow.units.relaxation_parameter_lu
+    if args.warmup:
+        f = orc.run("D3Q19", f, args.warmup, collision="bgk", tau=tau,
+                    strategy="PRE_STREAMING", nthreads=nthreads)
+    t0 = time.perf_counter()
+    orc.run("D3Q19", f, args.steps, collision="bgk", tau=tau, strategy="PRE_STREAMING",
+            nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    n = int(np.prod(res))
+    mlups = args.steps * n / dt / 1e6
+    sample = (f"{args.steps} steps of the oracle (C restatement of lettuce's torch step, "
+              f"float32, stream then collide) on a {res[0]}x{res[1]}x{res[2]} periodic TGV grid")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 3), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": res, "strategy": "PRE_STREAMING"},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": UNIT, "cores": nthreads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(mlups, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def time_variant(lt, torch, storage, pattern, steps, warmup, device):
+    """(ms per step from CUDA events, flow) for one storage/pattern"""
+    dtype = torch.float32
+    ctx = lt.Context(device, dtype, storage=storage)
+    flow = lt.TaylorGreenVortex(ctx, RES, RE, MA, lt.D3Q19)
+    tau = flow.units.relaxation_parameter_lu
+    if pattern == "aa":
+        sim = lt.Simulation(flow, lt.BGKCollision(tau), [], memory_pattern="aa")
+    else:
+        sim = lt.Simulation(flow, lt.BGKCollision(tau), [],
+                            streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+    stream = torch.cuda.current_stream(device)
+    for _ in range(warmup):
+        sim._collide_and_stream()
+    torch.cuda.synchronize(device)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        sim._collide_and_stream()
+    end.record(stream)
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    return ms, flow, sim
+
+
+def accuracy_fp16(lt, torch, device, steps=1000):
+    """relative L2 velocity error of fp16-shifted (and bf16) storage after
+    ``steps`` steps against a float64 run of the same workload"""
+    ref = lt.TaylorGreenVortex(lt.Context(device, torch.float64), RES, RE, MA, lt.D3Q19)
+    tau = ref.units.relaxation_parameter_lu
+    pre = lt.StreamingStrategy.PRE_STREAMING
+    lt.Simulation(ref, lt.BGKCollision(tau), [], pre)(steps)
+    u_ref = ref.u()
+    del ref
+    torch.cuda.empty_cache()
+    out = {}
+    for storage in ["fp16_shifted", None]:
+        low = lt.TaylorGreenVortex(lt.Context(device, torch.float32, storage=storage),
+                                   RES, RE, MA, lt.D3Q19)
+        lt.Simulation(low, lt.BGKCollision(tau), [], pre)(steps)
+        u = low.u().to(torch.float64)
+        err = (torch.linalg.vector_norm(u - u_ref) / torch.linalg.vector_norm(u_ref)).item()
+        out[storage or "f32"] = err
+        del low
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import lettuce_gb300 as lt
+    from lettuce_gb300 import build
+    build.build()
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    peak, peak_kind = peaks()
+    n_cells = int(np.prod(RES))
+
+    variants = {}
+    clocks = None
+    for key, storage, pattern in [("f32_pull", None, "pull"), ("f16s_pull", "fp16_shifted", "pull"),
+                                  ("f32_aa", None, "aa"), ("f16s_aa", "fp16_shifted", "aa")]:
+        barrier(world)
+        if key == "f32_pull":
+            with ClockSampler(local) as cs:
+                ms, flow, sim = time_variant(lt, torch, storage, pattern, args.steps,
+                                             args.warmup, device)
+            clocks = cs.summary()
+        else:
+            ms, flow, sim = time_variant(lt, torch, storage, pattern, args.steps,
+                                         args.warmup, device)
+        ms = allmax(ms, world, device)
+        bpc = BYTES_PER_CELL["f16" if storage else "f32"]
+        mlups = n_cells / (ms * 1e-3) / 1e6
+        achieved = bpc * n_cells / (ms * 1e-3) / 1e9
+        variants[key] = {"mlups": round(mlups * world, 1), "ms_per_step": round(ms, 4),
+                         "achieved_gbs": round(achieved, 1),
+                         "frac_of_peak": round(achieved / peak, 4)}
+        del flow, sim
+        torch.cuda.empty_cache()
+
+    head = variants["f32_pull"]
+    ms = head["ms_per_step"]
+    achieved = head["achieved_gbs"]
+    traffic = traffic_per_launch("step_kernel_d3q19_f32_pull_256")
+
+    # e2e: lettuce's user-level call on host data through the public API:
+    # pinned host populations -> flow.f (H2D) -> simulation(K) -> flow.f
+    # (D2H); per-step bytes are the copies amortised over the K steps
+    ctx = lt.Context(device, torch.float32)
+    flow = lt.TaylorGreenVortex(ctx, RES, RE, MA, lt.D3Q19)
+    host = flow.f.cpu().pin_memory()
+    back = torch.empty_like(host).pin_memory()
+    sim = lt.Simulation(flow, lt.BGKCollision(flow.units.relaxation_parameter_lu), [],
+                        streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+    flow.f = host.to(device, non_blocking=True)
+    sim(args.warmup)
+    torch.cuda.synchronize(device)
+    barrier(world)
+    t0 = time.perf_counter()
+    flow.f = host.to(device, non_blocking=True)
+    sim(args.steps)
+    back.copy_(flow.f, non_blocking=True)
+    torch.cuda.synchronize(device)
+    e2e_s = allmax(time.perf_counter() - t0, world, device)
+    e2e_mlups = args.steps * n_cells / e2e_s / 1e6 * world
+    fbytes = host.numel() * host.element_size()
+    del flow, sim, host, back
+    torch.cuda.empty_cache()
+
+    acc = None
+    if not args.no_accuracy:
+        acc = accuracy_fp16(lt, torch, device, steps=args.accuracy_steps)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        mlups_cpu, s, n, dt = oracle_mlups([256, 256, 64], args.cpu_seconds, nthreads)
+        cpu = {"value": round(mlups_cpu, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{s} steps of the oracle (C restatement of lettuce's torch step, "
+                         f"float32) on a 256x256x64 periodic TGV crop, {dt:.1f} s"}
+
+    if rank != 0:
+        return 0
+    f16 = variants["f16s_pull"]
+    line = {
+        "metric": METRIC, "value": head["mlups"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (analytic Taylor-Green initial field)",
+        "config": {"workload": WORKLOAD, "grid": RES, "stencil": "D3Q19",
+                   "collision": "BGK", "strategy": "PRE_STREAMING (pull, A-B)",
+                   "storage": "float32", "parallelism": f"replicas x{world}",
+                   "l2": "no flush: each step reads 1.27 GB and writes 1.27 GB (> 129 MB L2)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_kind": peak_kind, "bytes_per_cell": BYTES_PER_CELL["f32"]},
+        "fp16_shifted": {"mlups": f16["mlups"], "speedup_vs_f32": round(f16["mlups"] / head["mlups"], 3),
+                         "frac_of_peak": f16["frac_of_peak"], "achieved_gbs": f16["achieved_gbs"],
+                         "bytes_per_cell": BYTES_PER_CELL["f16"]},
+        "variants": variants,
+        "accuracy": None if acc is None else {
+            "steps": args.accuracy_steps, "reference": "float64 run of the same kernels",
+            "u_rel_l2_fp16_shifted": acc.get("fp16_shifted"), "u_rel_l2_f32": acc.get("f32")},
+        "e2e": {"value": round(e2e_mlups, 1), "unit": UNIT,
+                "h2d_bytes_per_step": int(fbytes / args.steps),
+                "d2h_bytes_per_step": int(fbytes / args.steps),
+                "call": f"flow.f = pinned host field; simulation({args.steps}); field back to "
+                        "pinned host"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=1000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank)
+        return run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

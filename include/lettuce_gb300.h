@@ -1,0 +1,145 @@
+/*
+ * lettuce_gb300 -- C ABI of the GB300 (sm_103a) lattice Boltzmann step.
+ *
+ * Plain C: device pointers, sizes and scalars only. Every call is
+ * asynchronous on the CUDA stream it is given (a cudaStream_t passed as
+ * void*, NULL = legacy default stream); nothing here allocates device memory
+ * or synchronises. Errors: a non-zero return code and a message from
+ * lgb_last_error(); no call traps or aborts on the device.
+ *
+ * Layout of a population field: lettuce's [Q, *resolution], C-contiguous,
+ * the last lettuce dimension fastest (lettuce/_flow.py:92). The q ordering is
+ * lettuce's (lettuce/ext/_stencil/*.py).
+ */
+#ifndef LETTUCE_GB300_H
+#define LETTUCE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LGB_ABI_VERSION 1
+#define LGB_MAX_SUBSTEPS 8
+
+/* stencils (lettuce/ext/_stencil/d1q3.py, d2q9.py, d3q15.py, d3q19.py, d3q27.py) */
+enum { LGB_D1Q3 = 1, LGB_D2Q9 = 2, LGB_D3Q15 = 3, LGB_D3Q19 = 4, LGB_D3Q27 = 5 };
+
+/* population storage. The *_SHIFTED formats hold f_q - w_q in 16 bits; the
+ * collision arithmetic runs in float32 for them and for LGB_F32, in float64
+ * for LGB_F64. */
+enum { LGB_F64 = 0, LGB_F32 = 1, LGB_F16_SHIFTED = 2, LGB_BF16_SHIFTED = 3 };
+
+/* collision operators (lettuce/ext/_collision/) */
+enum { LGB_NO_COLLISION = 0, LGB_BGK = 1, LGB_TRT = 2, LGB_KBC = 3 };
+
+/* substeps of the masked collide, in lettuce's order pre-boundaries,
+ * collision, post-boundaries (lettuce/_simulation.py:258-305) */
+enum {
+    LGB_SUB_COLLISION = 0,
+    LGB_SUB_BOUNCE_BACK = 1,       /* lettuce/ext/_boundary/bounce_back_boundary.py */
+    LGB_SUB_EQUILIBRIUM_PU = 2,    /* lettuce/ext/_boundary/equilibrium_boundary_pu.py */
+    LGB_SUB_ANTI_BOUNCE_BACK = 3,  /* lettuce/ext/_boundary/anti_bounce_back_outlet.py */
+    LGB_SUB_NONE = 4
+};
+
+/* memory access pattern of one launch. PULL is stream-then-collide
+ * (lettuce PRE_STREAMING), PUSH collide-then-stream (POST_STREAMING), LOCAL
+ * collide only (NO_STREAMING), STREAM_ONLY streams without collide. The
+ * AA pair runs in place (f_out == f_in): AA_EVEN collides and stores every
+ * population into its opposite slot, AA_ODD gathers from the neighbours'
+ * opposite slots and scatters to the neighbours; an EVEN+ODD pair equals two
+ * PUSH steps. AA_UNPACK copies a field left by AA_EVEN (stream pending) into
+ * a second field in natural layout, without collision. */
+enum {
+    LGB_PULL = 0, LGB_PUSH = 1, LGB_LOCAL = 2, LGB_AA_EVEN = 3, LGB_AA_ODD = 4,
+    LGB_STREAM_ONLY = 5, LGB_AA_UNPACK = 6
+};
+
+/* per-cell flag byte: low 5 bits = substep index (lettuce's
+ * no_collision_mask value); bit 7 = the cell has no-streaming bits */
+#define LGB_FLAG_INDEX_MASK 0x1f
+#define LGB_FLAG_NO_STREAM 0x80
+
+typedef struct {
+    int32_t kind;
+    /* anti-bounce-back: lettuce dimension of the outflow normal and its sign */
+    int32_t axis;
+    int32_t sign;
+    int32_t reserved;
+    /* equilibrium BC: density and velocity in lattice units, in the compute
+     * type (double for LGB_F64, float otherwise), broadcast by element
+     * strides per lettuce dimension (0 = broadcast) */
+    const void *rho;
+    const void *u;
+    int64_t rho_stride[3];
+    int64_t u_stride[4]; /* component, then lettuce dimensions */
+} lgb_substep;
+
+typedef struct {
+    int32_t abi_version;     /* LGB_ABI_VERSION */
+    int32_t stencil;
+    int32_t storage;
+    int32_t collision;
+    int32_t pattern;
+    int32_t res[3];          /* lettuce resolution; unused trailing dims = 1 */
+    double tau;              /* BGK tau, TRT tau_plus, KBC tau */
+    double tau_minus;        /* TRT */
+    const void *f_in;        /* [Q][N] in `storage` */
+    void *f_out;             /* [Q][N]; == f_in for LGB_LOCAL / AA patterns */
+    const uint8_t *flags;    /* [N] or NULL (no boundaries) */
+    const uint32_t *no_stream_bits; /* [N] bit q = population q does not stream */
+    int32_t n_sub;
+    int32_t collision_index;
+    lgb_substep sub[LGB_MAX_SUBSTEPS];
+    uint32_t *status;        /* optional device word; bit 0 set on a non-finite density */
+} lgb_step_desc;
+
+/* ABI version of the loaded library */
+int lgb_abi_version(void);
+/* message of the last failing call on this host thread ("" if none) */
+const char *lgb_last_error(void);
+
+/* One stream+collide step over the whole grid.
+ * Replaces the generated binding `cuda_native.lettuce(f, f_next, ncm, nsm,
+ * tau_inv, velocity_k, density_k, ...)` of lettuce/cuda_native/_template.py:47-53,
+ * 72-81 (body from lettuce/cuda_native/_default_code_gen.py:285-316) and the
+ * torch step lettuce/_simulation.py:148-166, 241-305 it reproduces. */
+int lgb_step(const lgb_step_desc *desc, void *stream);
+
+/* Density [N] and velocity [D][N] (lattice units) of a population field, in
+ * float64 when `storage` is LGB_F64 and float32 otherwise.
+ * Replaces lettuce/_flow.py:157-193 (Flow.rho / Flow.j / Flow.u).
+ * aa_pending != 0 reads a field left by an LGB_AA_EVEN launch (populations in
+ * their opposite slots, stream pending). */
+int lgb_moments(int32_t stencil, int32_t storage, const int32_t *res,
+                const void *f, int32_t aa_pending, void *rho, void *u,
+                void *stream);
+
+/* Float64 reductions of a population field into out[LGB_REDUCE_FIELDS]:
+ *   [0] sum of rho over the box,           [1] sum of 0.5*|u|^2 over the box,
+ *   [2] max |u|^2 over the box,            [3] cells with a non-finite rho,
+ *   [4] sum of rho over box cells where mask != 0 (mask may be NULL).
+ * The box is [lo, hi) per lettuce dimension. `scratch` must hold
+ * lgb_reduce_scratch_bytes() bytes of device memory.
+ * Replaces the per-report reductions of
+ * lettuce/ext/_reporter/observable_reporter.py:34-42 (IncompressibleKineticEnergy),
+ * :27-31 (MaximumVelocity), :140-158 (Mass) and lettuce/_flow.py:200-204. */
+#define LGB_REDUCE_FIELDS 5
+int64_t lgb_reduce_scratch_bytes(void);
+int lgb_reduce(int32_t stencil, int32_t storage, const int32_t *res,
+               const void *f, int32_t aa_pending, const int32_t *lo,
+               const int32_t *hi, const uint8_t *mask, double *out,
+               void *scratch, void *stream);
+
+/* Copy a population field between storage formats (for example float32
+ * values into LGB_F16_SHIFTED storage and back). Replaces the dtype casts of
+ * lettuce/_context.py:97-115 for the population field. */
+int lgb_convert(int32_t stencil, int32_t src_storage, const void *src,
+                int32_t dst_storage, void *dst, int64_t n_cells, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

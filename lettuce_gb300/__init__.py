@@ -1,0 +1,38 @@
+"""lettuce_gb300 -- a GB300-native (sm_103a) lattice Boltzmann step behind
+lettuce's plugin surface.
+
+The public names mirror lettuce's (``Context``, stencils, ``UnitConversion``,
+``Flow``, collisions, boundaries, ``Simulation``, reporters, flows), so a
+script written against lettuce's native path runs unchanged. The stepping
+is done by hand-written CUDA kernels in ``liblettuce_gb300.so``, reached
+through its C ABI (include/lettuce_gb300.h); there is no CPU or torch
+fallback for the step.
+"""
+from ._context import Context
+from ._stencil import D1Q3, D2Q9, D3Q15, D3Q19, D3Q27, Stencil, TorchStencil
+from ._unit import UnitConversion
+from ._flow import (Boundary, Equilibrium, Flow, QuadraticEquilibrium,
+                    initialize_f_neq, torch_gradient)
+from ._collision import BGKCollision, Collision, KBCCollision, NoCollision, TRTCollision
+from ._boundary import AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU
+from ._simulation import BreakableSimulation, Reporter, Simulation, StreamingStrategy
+from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporterBase,
+                        HighMaReporter, IncompressibleKineticEnergy, Mass,
+                        MaximumVelocity, NaNReporter, Observable, ObservableReporter)
+from ._flows import ExtFlow, Obstacle, TaylorGreenVortex
+from ._native import NativeBoundary, NativeCollision, NativeEquilibrium
+
+__version__ = "0.1.0"
+
+__all__ = [
+    "Context", "Stencil", "TorchStencil", "D1Q3", "D2Q9", "D3Q15", "D3Q19", "D3Q27",
+    "UnitConversion", "Flow", "Equilibrium", "QuadraticEquilibrium", "Boundary",
+    "initialize_f_neq", "torch_gradient", "Collision", "BGKCollision",
+    "TRTCollision", "KBCCollision", "NoCollision", "BounceBackBoundary",
+    "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "Simulation",
+    "BreakableSimulation", "StreamingStrategy", "Reporter", "Observable",
+    "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",
+    "Enstrophy", "EnergySpectrum", "Mass", "ErrorReporter", "FailureReporterBase",
+    "NaNReporter", "HighMaReporter", "ExtFlow", "TaylorGreenVortex", "Obstacle",
+    "NativeBoundary", "NativeCollision", "NativeEquilibrium",
+]

@@ -1,0 +1,132 @@
+"""Thin wrappers that call the C ABI on torch tensors (device memory and the
+current torch stream are PyTorch's; the arithmetic is the library's)."""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_scratch = {}
+
+
+def _require_cuda(t: torch.Tensor, what: str):
+    if not t.is_cuda:
+        raise RuntimeError(f"{what}: lettuce_gb300 runs on CUDA tensors only "
+                           f"(got a tensor on {t.device}); there is no CPU path")
+    if not t.is_contiguous():
+        raise RuntimeError(f"{what}: tensor must be contiguous")
+
+
+def storage_of(dtype: torch.dtype) -> int:
+    if dtype == torch.float64:
+        return _lib.F64
+    if dtype == torch.float32:
+        return _lib.F32
+    raise TypeError(f"no natural population storage for {dtype}")
+
+
+def stream_of(t: torch.Tensor) -> int:
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def moments(stencil_id: int, storage: int, res: Sequence[int], f: torch.Tensor,
+            aa_pending: bool, compute_dtype: torch.dtype):
+    """(rho [1, *res], u [D, *res]) of a population field on the device"""
+    _require_cuda(f, "moments")
+    L = _lib.load()
+    d = len(res)
+    rho = torch.empty([1] + list(res), device=f.device, dtype=compute_dtype)
+    u = torch.empty([d] + list(res), device=f.device, dtype=compute_dtype)
+    r3 = _lib.i32x3(res)
+    _lib.check(L.lgb_moments(stencil_id, storage, ctypes.cast(r3, ctypes.c_void_p),
+                             f.data_ptr(), int(bool(aa_pending)), rho.data_ptr(),
+                             u.data_ptr(), stream_of(f)), "lgb_moments")
+    return rho, u
+
+
+def scratch_for(device: torch.device) -> torch.Tensor:
+    key = (device.type, device.index)
+    buf = _scratch.get(key)
+    if buf is None:
+        n = _lib.load().lgb_reduce_scratch_bytes()
+        buf = torch.empty(int(n), dtype=torch.uint8, device=device)
+        _scratch[key] = buf
+    return buf
+
+
+def reduce(stencil_id: int, storage: int, res: Sequence[int], f: torch.Tensor,
+           aa_pending: bool, lo: Optional[Sequence[int]] = None,
+           hi: Optional[Sequence[int]] = None,
+           mask: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None
+           ) -> torch.Tensor:
+    """float64 [mass, 0.5*sum|u|^2, max|u|^2, non-finite cells, masked mass]
+    as a device tensor (no host synchronisation)"""
+    _require_cuda(f, "reduce")
+    L = _lib.load()
+    if out is None:
+        out = torch.empty(_lib.REDUCE_FIELDS, dtype=torch.float64, device=f.device)
+    r3 = _lib.i32x3(res)
+    lo3 = _lib.i32x3(lo) if lo is not None else None
+    hi3 = _lib.i32x3(hi) if hi is not None else None
+    mptr = None
+    if mask is not None:
+        _require_cuda(mask, "reduce mask")
+        assert mask.dtype == torch.uint8
+        mptr = mask.data_ptr()
+    scratch = scratch_for(f.device)
+    _lib.check(L.lgb_reduce(stencil_id, storage, ctypes.cast(r3, ctypes.c_void_p),
+                            f.data_ptr(), int(bool(aa_pending)),
+                            ctypes.cast(lo3, ctypes.c_void_p) if lo3 is not None else None,
+                            ctypes.cast(hi3, ctypes.c_void_p) if hi3 is not None else None,
+                            mptr, out.data_ptr(), scratch.data_ptr(), stream_of(f)),
+               "lgb_reduce")
+    return out
+
+
+def convert(stencil_id: int, src: torch.Tensor, src_storage: int, dst: torch.Tensor,
+            dst_storage: int, n_cells: int):
+    _require_cuda(src, "convert")
+    _require_cuda(dst, "convert")
+    L = _lib.load()
+    _lib.check(L.lgb_convert(stencil_id, src_storage, src.data_ptr(), dst_storage,
+                             dst.data_ptr(), int(n_cells), stream_of(src)), "lgb_convert")
+
+
+def step(desc: _lib.StepDesc, stream: int):
+    L = _lib.load()
+    _lib.check(L.lgb_step(ctypes.byref(desc), stream), "lgb_step")
+
+
+def new_desc(stencil_id: int, storage: int, res: Sequence[int]) -> _lib.StepDesc:
+    d = _lib.StepDesc()
+    d.abi_version = _lib.ABI_VERSION
+    d.stencil = stencil_id
+    d.storage = storage
+    for k, v in enumerate(list(res) + [1] * (3 - len(res))):
+        d.res[k] = int(v)
+    d.tau = 1.0
+    d.tau_minus = 1.0
+    return d
+
+
+def bcast_strides(t: torch.Tensor, full_shape: Sequence[int]) -> list:
+    """element strides of ``t`` broadcast to ``full_shape`` (0 where t has
+    size 1)"""
+    assert t.dim() == len(full_shape), (tuple(t.shape), tuple(full_shape))
+    out = []
+    for i, n in enumerate(full_shape):
+        if t.shape[i] == 1:
+            out.append(0)
+        elif t.shape[i] == n:
+            out.append(int(t.stride(i)))
+        else:
+            raise ValueError(f"shape {tuple(t.shape)} does not broadcast to {tuple(full_shape)}")
+    return out
+
+
+def as_numpy_f64(t: torch.Tensor) -> np.ndarray:
+    return t.detach().to(torch.float64).cpu().numpy()

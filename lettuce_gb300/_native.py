@@ -1,0 +1,47 @@
+"""Descriptors returned by the plugin hooks ``native_generator``.
+
+lettuce's hooks (lettuce/_simulation.py:17-28, lettuce/_flow.py:17-52) return
+code-emitting objects that the cuda_native generator turns into CUDA source
+at run time. Here the kernels are compiled ahead of time, so the same hooks
+return small descriptors: which operator, which substep index, and its
+scalar/tensor parameters. ``Simulation`` packs them into ``lgb_step_desc``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Optional
+
+import torch
+
+from . import _lib
+
+__all__ = ["NativeEquilibrium", "NativeQuadraticEquilibrium", "NativeCollision",
+           "NativeBoundary"]
+
+
+@dataclass
+class NativeEquilibrium:
+    name: str
+
+
+def NativeQuadraticEquilibrium() -> NativeEquilibrium:
+    return NativeEquilibrium("quadratic")
+
+
+@dataclass
+class NativeCollision:
+    kind: int                  # _lib.NO_COLLISION / BGK / TRT / KBC
+    index: int
+    tau: float = 1.0
+    tau_minus: float = 1.0
+
+
+@dataclass
+class NativeBoundary:
+    kind: int                  # _lib.SUB_BOUNCE_BACK / SUB_EQUILIBRIUM_PU / ...
+    index: int
+    rho: Optional[torch.Tensor] = None   # equilibrium BC, [1|N1, 1|N2, ...]
+    u: Optional[torch.Tensor] = None     # equilibrium BC, [1|D, 1|N1, ...]
+    axis: int = 0                        # anti-bounce-back
+    sign: int = 1
+    keep: list = field(default_factory=list)

@@ -1,0 +1,306 @@
+"""The step engine: lettuce's ``Simulation`` (lettuce/_simulation.py:42-344)
+driving the fused GB300 kernels.
+
+``Simulation.__init__`` builds lettuce's no-collision / no-streaming masks
+exactly as lettuce does (:100-146), packs them into one flag byte per cell
+plus a per-cell no-streaming bit word, and turns the collision and boundary
+plugins' ``native_generator`` descriptors into an ``lgb_step_desc``. Each
+step is then one (or, for DOUBLE_STREAMING, two) kernel launches on the
+current torch stream, with no host synchronisation inside the loop:
+
+* PRE_STREAMING  -> pull pattern (stream then collide, one pass)
+* POST_STREAMING -> push pattern, or the in-place AA pattern with
+                    ``memory_pattern="aa"`` (half the memory, same traffic)
+* NO_STREAMING   -> collide only
+* DOUBLE_STREAMING -> pull, then stream only
+"""
+from __future__ import annotations
+
+import warnings
+from abc import ABC, abstractmethod
+from enum import Enum
+from functools import lru_cache
+from timeit import default_timer as timer
+from typing import List, Optional
+
+import torch
+
+from . import _device, _lib
+from ._native import NativeBoundary, NativeCollision
+
+__all__ = ["Reporter", "Simulation", "BreakableSimulation", "StreamingStrategy",
+           "apply_local"]
+
+
+class StreamingStrategy(Enum):
+    """same values as lettuce/cuda_native/_default_code_gen.py:13-25"""
+    NO_STREAMING = 0b00
+    PRE_STREAMING = 0b10
+    POST_STREAMING = 0b01
+    DOUBLE_STREAMING = 0b11
+
+    @lru_cache
+    def pre_streaming(self) -> bool:
+        return bool(self.value & StreamingStrategy.PRE_STREAMING.value)
+
+    @lru_cache
+    def post_streaming(self) -> bool:
+        return bool(self.value & StreamingStrategy.POST_STREAMING.value)
+
+
+class Reporter(ABC):
+    interval: int
+
+    def __init__(self, interval: int):
+        self.interval = interval
+
+    @abstractmethod
+    def __call__(self, simulation: "Simulation"):
+        ...
+
+
+def _fill_substep(sub: _lib.Substep, native, keep: list, res):
+    if isinstance(native, NativeCollision):
+        sub.kind = _lib.SUB_COLLISION
+        return
+    sub.kind = native.kind
+    if native.kind == _lib.SUB_EQUILIBRIUM_PU:
+        rho, u = native.rho, native.u
+        rs = _device.bcast_strides(rho, list(res))
+        us = _device.bcast_strides(u, [u.shape[0]] + list(res))
+        keep += [rho, u]
+        sub.rho = rho.data_ptr()
+        sub.u = u.data_ptr()
+        for k in range(3):
+            sub.rho_stride[k] = rs[k] if k < len(rs) else 0
+        for k in range(4):
+            sub.u_stride[k] = us[k] if k < len(us) else 0
+    elif native.kind == _lib.SUB_ANTI_BOUNCE_BACK:
+        sub.axis = native.axis
+        sub.sign = native.sign
+
+
+def _desc_for(flow, natives, flags, nsb, collision_index):
+    """lgb_step_desc for a list of substep descriptors (collision included)"""
+    coll = natives[collision_index]
+    d = _device.new_desc(flow.stencil.lgb_id, flow.context.storage, flow.resolution)
+    d.collision = coll.kind
+    d.tau = coll.tau
+    d.tau_minus = coll.tau_minus
+    keep = []
+    if flags is not None:
+        if len(natives) > _lib.MAX_SUBSTEPS:
+            raise ValueError(f"at most {_lib.MAX_SUBSTEPS} substeps (boundaries + collision)")
+        d.flags = flags.data_ptr()
+        d.no_stream_bits = nsb.data_ptr() if nsb is not None else None
+        d.n_sub = len(natives)
+        d.collision_index = collision_index
+        for k, nat in enumerate(natives):
+            _fill_substep(d.sub[k], nat, keep, flow.resolution)
+    return d, keep
+
+
+def pack_masks(no_collision_mask: torch.Tensor, no_streaming_mask: torch.Tensor):
+    """(flags uint8 [*res], no-stream bits int32 [*res] or None).
+
+    flags = the no-collision index | 0x80 where the cell has any population
+    that does not stream; bit q of the word is set where lettuce's torch
+    stream keeps population q (``no_streaming_mask[q] == 1``,
+    lettuce/_simulation.py:254-255)."""
+    ncm = no_collision_mask.to(torch.uint8)
+    if int(ncm.max().item()) > _lib.FLAG_INDEX_MASK:
+        raise ValueError("too many substeps for the flag byte")
+    keep = no_streaming_mask == 1
+    keep[0] = False  # the rest population never streams anyway
+    q = keep.shape[0]
+    shifts = torch.arange(q, device=keep.device, dtype=torch.int64).view(
+        [-1] + [1] * (keep.dim() - 1))
+    bits = torch.sum(keep.to(torch.int64) << shifts, dim=0)
+    has = bits != 0
+    flags = ncm | (has.to(torch.uint8) * _lib.FLAG_NO_STREAM)
+    if not bool(has.any().item()):
+        return flags.contiguous(), None
+    return flags.contiguous(), bits.to(torch.int32).contiguous()
+
+
+def apply_local(flow, collision_native: NativeCollision,
+                boundary_native: Optional[NativeBoundary] = None,
+                flags: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """run the collide-only pattern once (out of place) and return the new
+    populations in the context dtype; used by direct calls of a collision or
+    boundary operator"""
+    if flow.context.device.type != "cuda":
+        raise RuntimeError("lettuce_gb300 operators run on CUDA devices only; "
+                           "there is no CPU path")
+    natives = [collision_native] + ([boundary_native] if boundary_native else [])
+    src = flow.f_raw if not flow._aa_pending else None
+    if src is None:
+        flow._unpack_aa()
+        src = flow.f_raw
+    out = torch.empty_like(src)
+    d, keep = _desc_for(flow, natives, flags, None, 0)
+    d.pattern = _lib.LOCAL
+    d.f_in = src.data_ptr()
+    d.f_out = out.data_ptr()
+    _device.step(d, _device.stream_of(src))
+    del keep
+    if flow.context.shifted:
+        w = flow.torch_stencil.w.to(torch.float32).view([-1] + [1] * flow.stencil.d)
+        return out.to(torch.float32) + w
+    return out
+
+
+class Simulation:
+    def __init__(self, flow, collision, reporter: List[Reporter],
+                 streaming_strategy=StreamingStrategy.POST_STREAMING,
+                 memory_pattern: str = "ab"):
+        self.flow = flow
+        flow.collision = collision
+        self.context = flow.context
+        self.collision = collision
+        pre = list(flow.pre_boundaries or [])
+        post = list(flow.post_boundaries or [])
+        self.pre_boundaries = pre
+        self.post_boundaries = post
+        self.collision_index = len(pre)
+        self.transformer = pre + [collision] + post
+        self.reporter = reporter
+        self.streaming_strategy = streaming_strategy
+        if memory_pattern not in ("ab", "aa"):
+            raise ValueError("memory_pattern is 'ab' (two fields) or 'aa' (in place)")
+        self.memory_pattern = memory_pattern
+        collision.bind(flow)
+
+        # masks, exactly as lettuce/_simulation.py:100-146 builds them
+        self.no_collision_mask = None
+        self.no_streaming_mask = None
+        shape_f = [flow.stencil.q, *flow.resolution]
+        if len(pre) + len(post) > 0:
+            self.no_collision_mask = self.context.full_tensor(
+                flow.resolution, self.collision_index, dtype=torch.uint8)
+            self.no_streaming_mask = self.context.full_tensor(
+                shape_f, self.collision_index, dtype=torch.uint8)
+            for i, b in list(enumerate(pre)) + list(enumerate(post, start=self.collision_index + 1)):
+                ncm = b.make_no_collision_mask(list(flow.resolution), context=self.context)
+                if ncm is not None:
+                    self.no_collision_mask[torch.as_tensor(ncm, device=self.context.device).bool()] = i
+                nsm = b.make_no_streaming_mask(shape_f, context=self.context)
+                if nsm is not None:
+                    self.no_streaming_mask |= torch.as_tensor(
+                        nsm, device=self.context.device).to(torch.uint8)
+
+        # native descriptors (no fallback: every component must have one)
+        missing = [c.__class__.__name__ for c in self.transformer if not c.native_available()]
+        if flow.equilibrium is not None and not flow.equilibrium.native_available():
+            missing.append(flow.equilibrium.__class__.__name__)
+        if missing:
+            raise NotImplementedError(
+                f"no GB300 kernel for {', '.join(missing)}; lettuce_gb300 has no torch fallback")
+        natives = [b.native_generator(i) for i, b in enumerate(pre)]
+        natives.append(collision.native_generator(self.collision_index))
+        natives += [b.native_generator(i)
+                    for i, b in enumerate(post, start=self.collision_index + 1)]
+        self._natives = natives
+
+        self._flags = self._nsb = None
+        if self.no_collision_mask is not None:
+            self._flags, self._nsb = pack_masks(self.no_collision_mask, self.no_streaming_mask)
+        self._desc, self._keep = _desc_for(flow, natives, self._flags, self._nsb,
+                                           self.collision_index)
+        self._status = None
+        if self.context.device.type == "cuda":
+            self._status = torch.zeros(1, dtype=torch.int32, device=self.context.device)
+            self._desc.status = self._status.data_ptr()
+
+        s = streaming_strategy
+        if memory_pattern == "aa":
+            if s != StreamingStrategy.POST_STREAMING:
+                raise ValueError("the AA pattern implements POST_STREAMING only")
+            if self._nsb is not None:
+                raise ValueError("the AA pattern does not support no-streaming masks "
+                                 "(anti-bounce-back outlets); use memory_pattern='ab'")
+        if s == StreamingStrategy.PRE_STREAMING:
+            self._patterns = [_lib.PULL]
+        elif s == StreamingStrategy.POST_STREAMING:
+            self._patterns = [_lib.PUSH]
+        elif s == StreamingStrategy.DOUBLE_STREAMING:
+            self._patterns = [_lib.PULL, _lib.STREAM_ONLY]
+        else:
+            self._patterns = [_lib.LOCAL]
+
+    # ------------------------------------------------------------------
+    @property
+    def units(self):
+        return self.flow.units
+
+    @property
+    def status(self) -> int:
+        """device status word (bit 0: a non-finite density was seen); reading
+        it synchronises with the device"""
+        return 0 if self._status is None else int(self._status.item())
+
+    def _require_device(self):
+        if self.context.device.type != "cuda":
+            raise RuntimeError("lettuce_gb300 steps on CUDA devices only; there is no CPU path")
+
+    def _collide_and_stream(self, *_, **__):
+        flow = self.flow
+        d = self._desc
+        stream = self.context.stream_handle()
+        if self.memory_pattern == "aa":
+            d.pattern = _lib.AA_ODD if flow._aa_pending else _lib.AA_EVEN
+            d.f_in = d.f_out = flow._f.data_ptr()
+            _device.step(d, stream)
+            flow._aa_pending = not flow._aa_pending
+            return
+        for pat in self._patterns:
+            src = flow._f
+            dst = flow.f_next
+            d.pattern = pat
+            d.f_in = src.data_ptr()
+            d.f_out = dst.data_ptr()
+            _device.step(d, stream)
+            flow._f, flow._f_next = dst, src
+
+    def step(self, num_steps: int):
+        warnings.warn("Simulation.step() is deprecated; call simulation(num_steps)",
+                      DeprecationWarning)
+        return self(num_steps)
+
+    def _report(self):
+        for reporter in self.reporter:
+            reporter(self)
+
+    def __call__(self, num_steps: int) -> float:
+        self._require_device()
+        beg = timer()
+        if self.flow.i == 0:
+            self._report()
+        for _ in range(num_steps):
+            self._collide_and_stream(self)
+            self.flow.i += 1
+            self._report()
+        self.context.synchronize()
+        end = timer()
+        return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)
+
+
+class BreakableSimulation(Simulation):
+    """stops when a reporter pushes flow.i past num_steps
+    (lettuce/_simulation.py:325-344)"""
+
+    def __init__(self, flow, collision, reporter: List[Reporter], **kwargs):
+        super().__init__(flow, collision, reporter, **kwargs)
+
+    def __call__(self, num_steps: int) -> float:
+        self._require_device()
+        beg = timer()
+        if self.flow.i == 0:
+            self._report()
+        while self.flow.i < num_steps:
+            self._collide_and_stream(self)
+            self.flow.i += 1
+            self._report()
+        self.context.synchronize()
+        end = timer()
+        return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)

@@ -1,0 +1,495 @@
+// extern "C" entry points of liblettuce_gb300.so (declared in
+// include/lettuce_gb300.h): argument validation, packing of the kernel
+// parameter block, dispatch to the per-stencil instantiations, and the
+// moment / reduction / conversion kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "lettuce_gb300.h"
+#include "lgb_step.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(const char *fmt, ...) __attribute__((format(printf, 1, 2)));
+int fail(const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return -1;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail("%s: %s", what, cudaGetErrorString(e));
+}
+
+int stencil_dq(int s, int *d, int *q) {
+    switch (s) {
+    case LGB_D1Q3: *d = 1; *q = 3; return 0;
+    case LGB_D2Q9: *d = 2; *q = 9; return 0;
+    case LGB_D3Q15: *d = 3; *q = 15; return 0;
+    case LGB_D3Q19: *d = 3; *q = 19; return 0;
+    case LGB_D3Q27: *d = 3; *q = 27; return 0;
+    }
+    return -1;
+}
+
+struct Grid {
+    int d, q;
+    uint32_t X, Y, Z, N;
+};
+
+int make_grid(int stencil, const int32_t *res, Grid *g) {
+    if (stencil_dq(stencil, &g->d, &g->q)) return fail("unknown stencil id %d", stencil);
+    if (!res) return fail("resolution pointer is NULL");
+    uint64_t r[3] = {1, 1, 1};
+    for (int i = 0; i < g->d; ++i) {
+        if (res[i] <= 0) return fail("resolution[%d] = %d must be positive", i, res[i]);
+        r[3 - g->d + i] = (uint64_t)res[i];
+    }
+    const uint64_t n = r[0] * r[1] * r[2];
+    if (n >= (1ull << 32)) return fail("grid of %llu cells exceeds the 2^32-1 cell limit",
+                                       (unsigned long long)n);
+    g->X = (uint32_t)r[0]; g->Y = (uint32_t)r[1]; g->Z = (uint32_t)r[2]; g->N = (uint32_t)n;
+    return 0;
+}
+
+bool valid_storage(int s) { return s >= LGB_F64 && s <= LGB_BF16_SHIFTED; }
+
+cudaError_t dispatch_step(int stencil, int storage, int coll, int pat, bool masked,
+                          const lgb::StepParams &p, cudaStream_t s) {
+#define LGB_STORAGE_SWITCH(name)                                            \
+    switch (storage) {                                                      \
+    case 0: return lgb::name##_s0(coll, pat, masked, p, s);                 \
+    case 1: return lgb::name##_s1(coll, pat, masked, p, s);                 \
+    case 2: return lgb::name##_s2(coll, pat, masked, p, s);                 \
+    case 3: return lgb::name##_s3(coll, pat, masked, p, s);                 \
+    }                                                                       \
+    return cudaErrorInvalidValue;
+    switch (stencil) {
+    case LGB_D1Q3: LGB_STORAGE_SWITCH(step_d1q3)
+    case LGB_D2Q9: LGB_STORAGE_SWITCH(step_d2q9)
+    case LGB_D3Q15: LGB_STORAGE_SWITCH(step_d3q15)
+    case LGB_D3Q19: LGB_STORAGE_SWITCH(step_d3q19)
+    case LGB_D3Q27: LGB_STORAGE_SWITCH(step_d3q27)
+    }
+#undef LGB_STORAGE_SWITCH
+    return cudaErrorInvalidValue;
+}
+
+// ----------------------------------------------------------------------------
+// moments
+
+template <int SID, int ST, bool AA>
+__global__ void __launch_bounds__(256) moments_kernel(const void *fv, uint32_t X, uint32_t Y,
+                                                      uint32_t Z, uint32_t N, lgb::FastDiv divZ,
+                                                      lgb::FastDiv divY, void *rho_v, void *u_v) {
+    using S = lgb::Stencil<SID>;
+    using Sto = lgb::Storage<ST>;
+    using R = typename Sto::R;
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    lgb::StepParams p;
+    p.X = X; p.Y = Y; p.Z = Z; p.N = N;
+    const uint32_t row = divZ.div(n), z = n - row * Z;
+    const uint32_t x = divY.div(row), y = row - x * Y;
+    lgb::Nbr c;
+    c.set(x, y, z, p);
+    R f[S::Q];
+    lgb::load_cell<S, Sto, AA ? lgb::LOAD_AA_ODD : lgb::LOAD_OWN, false>(
+        p, static_cast<const typename Sto::T *>(fv), c, n, 0u, f);
+    R rho, u[3];
+    lgb::cell_moments<S>(f, rho, u);
+    static_cast<R *>(rho_v)[n] = rho;
+#pragma unroll
+    for (int d = 0; d < S::D; ++d) static_cast<R *>(u_v)[(size_t)d * N + n] = u[d];
+}
+
+template <int SID, int ST>
+cudaError_t launch_moments(const Grid &g, const void *f, int aa, void *rho, void *u, cudaStream_t s) {
+    const unsigned blocks = (g.N + 255) / 256;
+    const lgb::FastDiv dz = lgb::FastDiv::make(g.Z), dy = lgb::FastDiv::make(g.Y);
+    if (aa)
+        moments_kernel<SID, ST, true><<<blocks, 256, 0, s>>>(f, g.X, g.Y, g.Z, g.N, dz, dy, rho, u);
+    else
+        moments_kernel<SID, ST, false><<<blocks, 256, 0, s>>>(f, g.X, g.Y, g.Z, g.N, dz, dy, rho, u);
+    return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------------------
+// float64 reductions: grid-stride partials per block into scratch, then a
+// single block folds the partials in a fixed order (deterministic result)
+
+constexpr int kReduceBlocks = 1216;  // 152 SMs x 8
+constexpr int kReduceThreads = 256;
+
+struct ReduceBox {
+    uint32_t lo[3], hi[3];  // internal X, Y, Z
+};
+
+__device__ __forceinline__ void block_fold(double (&v)[LGB_REDUCE_FIELDS], double *smem) {
+    // warp shuffles, then one value per warp through shared memory
+#pragma unroll
+    for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w = __shfl_down_sync(0xffffffffu, v[i], o);
+            v[i] = (i == 2) ? fmax(v[i], w) : v[i] + w;
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) smem[warp * LGB_REDUCE_FIELDS + i] = v[i];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) v[i] = lane < nw ? smem[lane * LGB_REDUCE_FIELDS + i] : (i == 2 ? 0.0 : 0.0);
+#pragma unroll
+        for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double w = __shfl_down_sync(0xffffffffu, v[i], o);
+                v[i] = (i == 2) ? fmax(v[i], w) : v[i] + w;
+            }
+        }
+    }
+}
+
+template <int SID, int ST, bool AA>
+__global__ void __launch_bounds__(kReduceThreads) reduce_partials_kernel(
+    const void *fv, uint32_t X, uint32_t Y, uint32_t Z, uint32_t N, lgb::FastDiv divZ,
+    lgb::FastDiv divY, ReduceBox box, const uint8_t *mask, double *partials) {
+    using S = lgb::Stencil<SID>;
+    using Sto = lgb::Storage<ST>;
+    using R = typename Sto::R;
+    __shared__ double smem[(kReduceThreads / 32) * LGB_REDUCE_FIELDS];
+    lgb::StepParams p;
+    p.X = X; p.Y = Y; p.Z = Z; p.N = N;
+    double v[LGB_REDUCE_FIELDS] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t n = (uint32_t)i;
+        const uint32_t row = divZ.div(n), z = n - row * Z;
+        const uint32_t x = divY.div(row), y = row - x * Y;
+        if (x < box.lo[0] || x >= box.hi[0] || y < box.lo[1] || y >= box.hi[1] || z < box.lo[2] ||
+            z >= box.hi[2])
+            continue;
+        lgb::Nbr c;
+        c.set(x, y, z, p);
+        R f[S::Q];
+        lgb::load_cell<S, Sto, AA ? lgb::LOAD_AA_ODD : lgb::LOAD_OWN, false>(
+            p, static_cast<const typename Sto::T *>(fv), c, n, 0u, f);
+        double rho = 0.0, j[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) {
+            const double fq = (double)f[q];
+            rho += fq;
+#pragma unroll
+            for (int d = 0; d < S::D; ++d) j[d] += (double)S::e(q, d) * fq;
+        }
+        if (!isfinite(rho)) {
+            v[3] += 1.0;
+            continue;
+        }
+        double uu = 0.0;
+#pragma unroll
+        for (int d = 0; d < S::D; ++d) uu += (j[d] / rho) * (j[d] / rho);
+        v[0] += rho;
+        v[1] += 0.5 * uu;
+        v[2] = fmax(v[2], uu);
+        if (mask && mask[n]) v[4] += rho;
+    }
+    block_fold(v, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) partials[blockIdx.x * LGB_REDUCE_FIELDS + i] = v[i];
+    }
+}
+
+__global__ void __launch_bounds__(kReduceThreads) reduce_final_kernel(const double *partials, int nblocks,
+                                                                      double *out) {
+    __shared__ double smem[(kReduceThreads / 32) * LGB_REDUCE_FIELDS];
+    double v[LGB_REDUCE_FIELDS] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+        for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) {
+            const double w = partials[b * LGB_REDUCE_FIELDS + i];
+            v[i] = (i == 2) ? fmax(v[i], w) : v[i] + w;
+        }
+    }
+    block_fold(v, smem);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < LGB_REDUCE_FIELDS; ++i) out[i] = v[i];
+    }
+}
+
+template <int SID, int ST>
+cudaError_t launch_reduce(const Grid &g, const void *f, int aa, const ReduceBox &box,
+                          const uint8_t *mask, double *out, double *partials, cudaStream_t s) {
+    const lgb::FastDiv dz = lgb::FastDiv::make(g.Z), dy = lgb::FastDiv::make(g.Y);
+    if (aa)
+        reduce_partials_kernel<SID, ST, true><<<kReduceBlocks, kReduceThreads, 0, s>>>(
+            f, g.X, g.Y, g.Z, g.N, dz, dy, box, mask, partials);
+    else
+        reduce_partials_kernel<SID, ST, false><<<kReduceBlocks, kReduceThreads, 0, s>>>(
+            f, g.X, g.Y, g.Z, g.N, dz, dy, box, mask, partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    reduce_final_kernel<<<1, kReduceThreads, 0, s>>>(partials, kReduceBlocks, out);
+    return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------------------
+// storage conversion
+
+template <int SID, int SRC, int DST>
+__global__ void __launch_bounds__(256) convert_kernel(const void *src, void *dst, uint64_t n_cells) {
+    using S = lgb::Stencil<SID>;
+    const uint64_t total = n_cells * (uint64_t)S::Q;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(i / n_cells);
+        double w = 0.0;
+#pragma unroll
+        for (int k = 0; k < S::Q; ++k)
+            if (k == q) w = S::w(k);
+        const auto v = lgb::Storage<SRC>::load_plain(static_cast<const typename lgb::Storage<SRC>::T *>(src) + i, w);
+        lgb::Storage<DST>::store(static_cast<typename lgb::Storage<DST>::T *>(dst) + i,
+                                 (typename lgb::Storage<DST>::R)v, w);
+    }
+}
+
+template <int SID, int SRC>
+cudaError_t launch_convert_dst(int dst_st, const void *src, void *dst, uint64_t n, cudaStream_t s) {
+    const unsigned blocks = 152 * 16;
+    switch (dst_st) {
+    case LGB_F64: convert_kernel<SID, SRC, LGB_F64><<<blocks, 256, 0, s>>>(src, dst, n); break;
+    case LGB_F32: convert_kernel<SID, SRC, LGB_F32><<<blocks, 256, 0, s>>>(src, dst, n); break;
+    case LGB_F16_SHIFTED: convert_kernel<SID, SRC, LGB_F16_SHIFTED><<<blocks, 256, 0, s>>>(src, dst, n); break;
+    case LGB_BF16_SHIFTED: convert_kernel<SID, SRC, LGB_BF16_SHIFTED><<<blocks, 256, 0, s>>>(src, dst, n); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int SID>
+cudaError_t launch_convert(int src_st, const void *src, int dst_st, void *dst, uint64_t n, cudaStream_t s) {
+    switch (src_st) {
+    case LGB_F64: return launch_convert_dst<SID, LGB_F64>(dst_st, src, dst, n, s);
+    case LGB_F32: return launch_convert_dst<SID, LGB_F32>(dst_st, src, dst, n, s);
+    case LGB_F16_SHIFTED: return launch_convert_dst<SID, LGB_F16_SHIFTED>(dst_st, src, dst, n, s);
+    case LGB_BF16_SHIFTED: return launch_convert_dst<SID, LGB_BF16_SHIFTED>(dst_st, src, dst, n, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// stencil x storage switch for the templated helpers above
+#define LGB_SWITCH_SS(stencil, storage, CALL)                                        \
+    switch (stencil) {                                                               \
+    case LGB_D1Q3: switch (storage) { case 0: return CALL(LGB_D1Q3, 0); case 1: return CALL(LGB_D1Q3, 1); case 2: return CALL(LGB_D1Q3, 2); case 3: return CALL(LGB_D1Q3, 3); } break; \
+    case LGB_D2Q9: switch (storage) { case 0: return CALL(LGB_D2Q9, 0); case 1: return CALL(LGB_D2Q9, 1); case 2: return CALL(LGB_D2Q9, 2); case 3: return CALL(LGB_D2Q9, 3); } break; \
+    case LGB_D3Q15: switch (storage) { case 0: return CALL(LGB_D3Q15, 0); case 1: return CALL(LGB_D3Q15, 1); case 2: return CALL(LGB_D3Q15, 2); case 3: return CALL(LGB_D3Q15, 3); } break; \
+    case LGB_D3Q19: switch (storage) { case 0: return CALL(LGB_D3Q19, 0); case 1: return CALL(LGB_D3Q19, 1); case 2: return CALL(LGB_D3Q19, 2); case 3: return CALL(LGB_D3Q19, 3); } break; \
+    case LGB_D3Q27: switch (storage) { case 0: return CALL(LGB_D3Q27, 0); case 1: return CALL(LGB_D3Q27, 1); case 2: return CALL(LGB_D3Q27, 2); case 3: return CALL(LGB_D3Q27, 3); } break; \
+    }
+
+cudaError_t moments_dispatch(int stencil, int storage, const Grid &g, const void *f, int aa,
+                             void *rho, void *u, cudaStream_t s) {
+#define CALL(SID, ST) launch_moments<SID, ST>(g, f, aa, rho, u, s)
+    LGB_SWITCH_SS(stencil, storage, CALL)
+#undef CALL
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t reduce_dispatch(int stencil, int storage, const Grid &g, const void *f, int aa,
+                            const ReduceBox &box, const uint8_t *mask, double *out,
+                            double *partials, cudaStream_t s) {
+#define CALL(SID, ST) launch_reduce<SID, ST>(g, f, aa, box, mask, out, partials, s)
+    LGB_SWITCH_SS(stencil, storage, CALL)
+#undef CALL
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t convert_dispatch(int stencil, int src_st, const void *src, int dst_st, void *dst,
+                             uint64_t n, cudaStream_t s) {
+    switch (stencil) {
+    case LGB_D1Q3: return launch_convert<LGB_D1Q3>(src_st, src, dst_st, dst, n, s);
+    case LGB_D2Q9: return launch_convert<LGB_D2Q9>(src_st, src, dst_st, dst, n, s);
+    case LGB_D3Q15: return launch_convert<LGB_D3Q15>(src_st, src, dst_st, dst, n, s);
+    case LGB_D3Q19: return launch_convert<LGB_D3Q19>(src_st, src, dst_st, dst, n, s);
+    case LGB_D3Q27: return launch_convert<LGB_D3Q27>(src_st, src, dst_st, dst, n, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgb_abi_version(void) { return LGB_ABI_VERSION; }
+
+const char *lgb_last_error(void) { return g_last_error.c_str(); }
+
+int lgb_step(const lgb_step_desc *d, void *stream) {
+    if (!d) return fail("lgb_step: descriptor is NULL");
+    if (d->abi_version != LGB_ABI_VERSION)
+        return fail("lgb_step: descriptor ABI version %d, library %d", d->abi_version, LGB_ABI_VERSION);
+    Grid g;
+    if (make_grid(d->stencil, d->res, &g)) return -1;
+    if (!valid_storage(d->storage)) return fail("lgb_step: unknown storage id %d", d->storage);
+    if (d->collision < LGB_NO_COLLISION || d->collision > LGB_KBC)
+        return fail("lgb_step: unknown collision id %d", d->collision);
+    if (d->collision == LGB_KBC && !(d->stencil == LGB_D2Q9 || d->stencil == LGB_D3Q27))
+        return fail("lgb_step: KBC collision is only defined for D2Q9 and D3Q27");
+    if (d->pattern < LGB_PULL || d->pattern > LGB_AA_UNPACK)
+        return fail("lgb_step: unknown access pattern %d", d->pattern);
+    if (!d->f_in || !d->f_out) return fail("lgb_step: population pointer is NULL");
+    const bool in_place_ok = d->pattern == LGB_LOCAL || d->pattern == LGB_AA_EVEN || d->pattern == LGB_AA_ODD;
+    if (!in_place_ok && d->f_in == d->f_out)
+        return fail("lgb_step: pattern %d needs distinct input and output fields", d->pattern);
+    if (d->collision != LGB_NO_COLLISION && !(d->tau > 0.0))
+        return fail("lgb_step: relaxation time must be positive (got %g)", d->tau);
+    if (d->collision == LGB_TRT && !(d->tau_minus > 0.0))
+        return fail("lgb_step: TRT tau_minus must be positive (got %g)", d->tau_minus);
+
+    lgb::StepParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.f_in = d->f_in;
+    p.f_out = d->f_out;
+    p.X = g.X; p.Y = g.Y; p.Z = g.Z; p.N = g.N;
+    p.divZ = lgb::FastDiv::make(g.Z);
+    p.divY = lgb::FastDiv::make(g.Y);
+    p.cp.omega = 1.0 / d->tau;
+    p.cp.inv_2tp = 1.0 / (2.0 * d->tau);
+    p.cp.inv_2tm = d->collision == LGB_TRT ? 1.0 / (2.0 * d->tau_minus) : 0.0;
+    p.cp.beta = 1.0 / (2.0 * d->tau);
+    p.status = d->status;
+    p.abb_k = -1;
+    const bool masked = d->flags != nullptr;
+    if (masked && d->pattern == LGB_AA_UNPACK)
+        return fail("lgb_step: AA_UNPACK takes no boundary flags");
+    if (masked) {
+        if (d->n_sub < 1 || d->n_sub > LGB_MAX_SUBSTEPS)
+            return fail("lgb_step: %d substeps (1..%d supported)", d->n_sub, LGB_MAX_SUBSTEPS);
+        if (d->collision_index < 0 || d->collision_index >= d->n_sub ||
+            d->sub[d->collision_index].kind != LGB_SUB_COLLISION)
+            return fail("lgb_step: collision_index %d does not name the collision substep",
+                        d->collision_index);
+        p.flags = d->flags;
+        p.nsb = d->no_stream_bits;
+        p.has_nsm = d->no_stream_bits != nullptr;
+        if (p.has_nsm && (d->pattern == LGB_AA_EVEN || d->pattern == LGB_AA_ODD))
+            return fail("lgb_step: no-streaming masks are not supported by the AA pattern");
+        p.n_sub = d->n_sub;
+        const int off = 3 - g.d;
+        for (int k = 0; k < d->n_sub; ++k) {
+            const lgb_substep &s = d->sub[k];
+            lgb::SubParams &t = p.sub[k];
+            if (s.kind < LGB_SUB_COLLISION || s.kind > LGB_SUB_NONE)
+                return fail("lgb_step: substep %d has unknown kind %d", k, s.kind);
+            if (s.kind == LGB_SUB_COLLISION && k != d->collision_index)
+                return fail("lgb_step: substep %d is a second collision", k);
+            t.kind = s.kind;
+            if (s.kind == LGB_SUB_EQUILIBRIUM_PU) {
+                if (!s.rho || !s.u) return fail("lgb_step: equilibrium substep %d lacks rho/u", k);
+                t.rho = s.rho;
+                t.u = s.u;
+                t.us[0] = s.u_stride[0];
+                for (int i = 0; i < g.d; ++i) {
+                    t.rs[off + i] = s.rho_stride[i];
+                    t.us[1 + off + i] = s.u_stride[1 + i];
+                }
+            }
+            if (s.kind == LGB_SUB_ANTI_BOUNCE_BACK) {
+                if (p.abb_k >= 0) return fail("lgb_step: more than one anti-bounce-back outlet");
+                if (s.axis < 0 || s.axis >= g.d || (s.sign != 1 && s.sign != -1))
+                    return fail("lgb_step: outlet direction (axis %d, sign %d) invalid", s.axis, s.sign);
+                const int ia = off + s.axis;
+                const uint32_t n_ax = ia == 0 ? g.X : (ia == 1 ? g.Y : g.Z);
+                if (n_ax < 2) return fail("lgb_step: outlet needs at least 2 cells along its normal");
+                p.abb_k = k;
+                p.abb_axis = ia;
+                p.abb_sign = s.sign;
+                p.abb_plane = s.sign > 0 ? n_ax - 1 : 0;
+                p.abb_nb = s.sign > 0 ? n_ax - 2 : 1;
+            }
+        }
+    }
+    if (p.abb_k >= 0 && d->f_in == d->f_out)
+        return fail("lgb_step: the anti-bounce-back outlet reads its neighbour plane and "
+                    "needs distinct input and output fields");
+    cudaError_t e = dispatch_step(d->stencil, d->storage, d->collision, d->pattern, masked, p,
+                                  static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "lgb_step: launch failed");
+    return 0;
+}
+
+int lgb_moments(int32_t stencil, int32_t storage, const int32_t *res, const void *f,
+                int32_t aa_pending, void *rho, void *u, void *stream) {
+    Grid g;
+    if (make_grid(stencil, res, &g)) return -1;
+    if (!valid_storage(storage)) return fail("lgb_moments: unknown storage id %d", storage);
+    if (!f || !rho || !u) return fail("lgb_moments: NULL pointer");
+    cudaError_t e = moments_dispatch(stencil, storage, g, f, aa_pending, rho, u,
+                                     static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "lgb_moments: launch failed");
+    return 0;
+}
+
+int64_t lgb_reduce_scratch_bytes(void) {
+    return (int64_t)kReduceBlocks * LGB_REDUCE_FIELDS * (int64_t)sizeof(double);
+}
+
+int lgb_reduce(int32_t stencil, int32_t storage, const int32_t *res, const void *f,
+               int32_t aa_pending, const int32_t *lo, const int32_t *hi, const uint8_t *mask,
+               double *out, void *scratch, void *stream) {
+    Grid g;
+    if (make_grid(stencil, res, &g)) return -1;
+    if (!valid_storage(storage)) return fail("lgb_reduce: unknown storage id %d", storage);
+    if (!f || !out || !scratch) return fail("lgb_reduce: NULL pointer");
+    ReduceBox box;
+    const uint32_t full[3] = {g.X, g.Y, g.Z};
+    for (int i = 0; i < 3; ++i) { box.lo[i] = 0; box.hi[i] = full[i]; }
+    const int off = 3 - g.d;
+    for (int i = 0; i < g.d; ++i) {
+        const int32_t l = lo ? lo[i] : 0, h = hi ? hi[i] : (int32_t)full[off + i];
+        if (l < 0 || h > (int32_t)full[off + i] || l > h)
+            return fail("lgb_reduce: box [%d, %d) invalid along dimension %d", l, h, i);
+        box.lo[off + i] = (uint32_t)l;
+        box.hi[off + i] = (uint32_t)h;
+    }
+    cudaError_t e = reduce_dispatch(stencil, storage, g, f, aa_pending, box, mask, out,
+                                    static_cast<double *>(scratch), static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "lgb_reduce: launch failed");
+    return 0;
+}
+
+int lgb_convert(int32_t stencil, int32_t src_storage, const void *src, int32_t dst_storage,
+                void *dst, int64_t n_cells, void *stream) {
+    int dd, q;
+    if (stencil_dq(stencil, &dd, &q)) return fail("lgb_convert: unknown stencil id %d", stencil);
+    if (!valid_storage(src_storage) || !valid_storage(dst_storage))
+        return fail("lgb_convert: unknown storage id");
+    if (!src || !dst) return fail("lgb_convert: NULL pointer");
+    if (n_cells < 0) return fail("lgb_convert: negative cell count");
+    if (n_cells == 0) return 0;
+    cudaError_t e = convert_dispatch(stencil, src_storage, src, dst_storage, dst, (uint64_t)n_cells,
+                                     static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "lgb_convert: launch failed");
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,350 @@
+// Generic fused lattice Boltzmann step: one thread per cell, populations in
+// registers, every access pattern of the C ABI (pull / push / local / AA
+// even / AA odd / stream only) and lettuce's masked substep sequence.
+//
+// Semantics reproduced (lettuce/_simulation.py):
+//   * stream (:241-256): f[q](x) <- f[q](x - e_q), periodic wrap; where the
+//     no-streaming mask of (q, x) is set the destination keeps its value.
+//   * masked collide (:258-305): substeps k = 0..n-1 (pre-boundaries,
+//     collision, post-boundaries); a cell runs the substep whose index its
+//     no-collision mask holds. The anti-bounce-back outlet mutates its plane
+//     in place whatever that index is (anti_bounce_back_outlet.py:71-91), at
+//     its position in the sequence, reading the neighbour plane's velocity
+//     as it stands after the substeps before it.
+//   * PRE_STREAMING = stream then collide, POST_STREAMING = collide then
+//     stream (:148-166).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lgb_collide.cuh"
+#include "lgb_storage.cuh"
+
+namespace lgb {
+
+struct FastDiv {
+    uint32_t d, m, s;
+    static FastDiv make(uint32_t d) {
+        FastDiv f;
+        f.d = d;
+        uint32_t l = 0;
+        while ((1ull << l) < d) ++l;
+        f.s = l;
+        f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+        return f;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const {
+        if (s == 0) return n;
+        const uint32_t t = __umulhi(m, n);
+        return (t + ((n - t) >> 1)) >> (s - 1);
+    }
+};
+
+struct SubParams {
+    int32_t kind;
+    int32_t pad;
+    const void *rho;  // equilibrium BC density (compute type)
+    const void *u;    // equilibrium BC velocity (compute type)
+    int64_t rs[3];    // density strides, internal X, Y, Z
+    int64_t us[4];    // velocity strides: component, internal X, Y, Z
+};
+
+struct StepParams {
+    const void *f_in;
+    void *f_out;
+    uint32_t X, Y, Z, N;
+    FastDiv divZ, divY;
+    CollideParams cp;
+    const uint8_t *flags;
+    const uint32_t *nsb;
+    int32_t has_nsm;
+    int32_t n_sub;
+    // the anti-bounce-back outlet (at most one): its substep index (-1 for
+    // none), internal axis of its normal (0=X, 1=Y, 2=Z), sign, plane and
+    // neighbour-plane coordinates along that axis
+    int32_t abb_k, abb_axis, abb_sign;
+    uint32_t abb_plane, abb_nb;
+    SubParams sub[LGB_MAX_SUBSTEPS];
+    uint32_t *status;
+};
+
+// coordinates of a cell and of its periodic neighbours
+struct Nbr {
+    uint32_t x, y, z, xm, xp, ym, yp, zm, zp;
+    __device__ __forceinline__ void set(uint32_t x_, uint32_t y_, uint32_t z_, const StepParams &p) {
+        x = x_; y = y_; z = z_;
+        xm = x == 0 ? p.X - 1 : x - 1; xp = x + 1 == p.X ? 0 : x + 1;
+        ym = y == 0 ? p.Y - 1 : y - 1; yp = y + 1 == p.Y ? 0 : y + 1;
+        zm = z == 0 ? p.Z - 1 : z - 1; zp = z + 1 == p.Z ? 0 : z + 1;
+    }
+    // cell index of (x, y, z) + (dx, dy, dz), each in {-1, 0, 1}
+    __device__ __forceinline__ uint32_t at(int dx, int dy, int dz, const StepParams &p) const {
+        const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
+        const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
+        const uint32_t c = dz == 0 ? z : (dz > 0 ? zp : zm);
+        return (a * p.Y + b) * p.Z + c;
+    }
+};
+
+enum LoadKind { LOAD_OWN, LOAD_PULL, LOAD_AA_ODD };
+
+template <int PAT> struct PatternTraits;
+template <> struct PatternTraits<LGB_PULL> { static constexpr int load = LOAD_PULL; };
+template <> struct PatternTraits<LGB_STREAM_ONLY> { static constexpr int load = LOAD_PULL; };
+template <> struct PatternTraits<LGB_PUSH> { static constexpr int load = LOAD_OWN; };
+template <> struct PatternTraits<LGB_LOCAL> { static constexpr int load = LOAD_OWN; };
+template <> struct PatternTraits<LGB_AA_EVEN> { static constexpr int load = LOAD_OWN; };
+template <> struct PatternTraits<LGB_AA_ODD> { static constexpr int load = LOAD_AA_ODD; };
+template <> struct PatternTraits<LGB_AA_UNPACK> { static constexpr int load = LOAD_AA_ODD; };
+
+// populations of the cell `c` (index n) as the collide phase sees them
+template <class S, class Sto, int LOAD, bool MASKED>
+__device__ __forceinline__ void load_cell(const StepParams &p, const typename Sto::T *__restrict__ fin,
+                                          const Nbr &c, uint32_t n, uint32_t nsbits,
+                                          typename Sto::R (&f)[S::Q]) {
+    const size_t N = p.N;
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        uint32_t src = n;
+        int slot = q;
+        if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
+            src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
+            if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
+            if (MASKED && LOAD == LOAD_PULL && q != 0 && ((nsbits >> q) & 1u)) src = n;
+        }
+        f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
+    }
+}
+
+// the substep with index `idx`, copied out of the parameter block by an
+// unrolled select so no dynamic indexing of kernel parameters is needed
+__device__ __forceinline__ SubParams select_sub(const StepParams &p, int idx) {
+    SubParams r;
+    r.kind = LGB_SUB_NONE;
+    r.rho = nullptr;
+    r.u = nullptr;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) r.rs[d] = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) r.us[d] = 0;
+#pragma unroll
+    for (int k = 0; k < LGB_MAX_SUBSTEPS; ++k) {
+        if (k == idx && k < p.n_sub) {
+            r.kind = p.sub[k].kind;
+            r.rho = p.sub[k].rho;
+            r.u = p.sub[k].u;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) r.rs[d] = p.sub[k].rs[d];
+#pragma unroll
+            for (int d = 0; d < 4; ++d) r.us[d] = p.sub[k].us[d];
+        }
+    }
+    return r;
+}
+
+// substep `sb` (collision, bounce-back, equilibrium BC or none) at one cell
+template <class S, int COLL, class R>
+__device__ __forceinline__ void apply_local_substep(const StepParams &p, const SubParams &sb,
+                                                    const Nbr &c, R (&f)[S::Q]) {
+    if (sb.kind == LGB_SUB_COLLISION) {
+        R r;
+        collide<COLL, S>(f, p.cp, r);
+    } else if (sb.kind == LGB_SUB_BOUNCE_BACK) {
+        // bounce_back_boundary.py:17-18: f <- f[opposite]
+#pragma unroll
+        for (int q = 1; q < S::Q; ++q) {
+            const int o = S::opp(q);
+            if (q < o) { const R t = f[q]; f[q] = f[o]; f[o] = t; }
+        }
+    } else if (sb.kind == LGB_SUB_EQUILIBRIUM_PU) {
+        // equilibrium_boundary_pu.py:79-84: f <- feq(rho(p), u)
+        const R *rp = static_cast<const R *>(sb.rho);
+        const R *up = static_cast<const R *>(sb.u);
+        const R rho = rp[(int64_t)c.x * sb.rs[0] + (int64_t)c.y * sb.rs[1] + (int64_t)c.z * sb.rs[2]];
+        const int64_t ub = (int64_t)c.x * sb.us[1] + (int64_t)c.y * sb.us[2] + (int64_t)c.z * sb.us[3];
+        R u[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] = d < S::D ? up[ub + d * sb.us[0]] : R(0);
+        set_equilibrium<S>(f, rho, u);
+    }
+}
+
+__device__ __forceinline__ uint32_t coord_along(const Nbr &c, int axis) {
+    return axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+}
+
+// anti_bounce_back_outlet.py:71-91 at a cell of the outlet plane: the
+// neighbour one cell inside is rebuilt as the collide phase sees it at
+// substep abb_k (its populations after the substeps before abb_k).
+template <class S, int COLL, int LOAD, bool MASKED, class Sto>
+__device__ __forceinline__ void apply_outlet(const StepParams &p, const typename Sto::T *__restrict__ fin,
+                                             const Nbr &c, typename Sto::R (&f)[S::Q]) {
+    using R = typename Sto::R;
+    uint32_t xn = c.x, yn = c.y, zn = c.z;
+    if (p.abb_axis == 0) xn = p.abb_nb; else if (p.abb_axis == 1) yn = p.abb_nb; else zn = p.abb_nb;
+    Nbr cn;
+    cn.set(xn, yn, zn, p);
+    const uint32_t nn = (xn * p.Y + yn) * p.Z + zn;
+    const uint8_t fl = p.flags[nn];
+    const uint32_t nsb = ((fl & LGB_FLAG_NO_STREAM) && p.nsb) ? p.nsb[nn] : 0u;
+    R g[S::Q];
+    load_cell<S, Sto, LOAD, MASKED>(p, fin, cn, nn, nsb, g);
+    const int idx = fl & LGB_FLAG_INDEX_MASK;
+    if (idx < p.abb_k) apply_local_substep<S, COLL>(p, select_sub(p, idx), cn, g);
+    R rho, u[3], rn, un[3];
+    cell_moments<S>(f, rho, u);
+    cell_moments<S>(g, rn, un);
+    R uw[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) uw[d] = u[d] + R(0.5) * (u[d] - un[d]);
+    const R uu = dot_uu<S>(uw);
+#pragma unroll
+    for (int q = 1; q < S::Q; ++q) {
+        const int along = p.abb_axis == 0 ? ix<S>(q) : (p.abb_axis == 1 ? iy<S>(q) : iz<S>(q));
+        if (along * p.abb_sign == 1) {
+            R eu = R(0);
+#pragma unroll
+            for (int d = 0; d < S::D; ++d) eu += R(S::e(q, d)) * uw[d];
+            // cs^-4 = 9, cs^-2 = 3
+            f[S::opp(q)] = -f[q] + R(S::w(q)) * rho * (R(2) + eu * eu * R(9) - uu * R(3));
+        }
+    }
+}
+
+template <int SID, int ST, int COLL, int PAT, bool MASKED>
+__global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
+    using S = Stencil<SID>;
+    using Sto = Storage<ST>;
+    using R = typename Sto::R;
+    using T = typename Sto::T;
+    constexpr int LOAD = PatternTraits<PAT>::load;
+    const T *__restrict__ fin = static_cast<const T *>(p.f_in);
+    T *fout = static_cast<T *>(p.f_out);
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.N) return;
+    const uint32_t row = p.divZ.div(n);
+    const uint32_t z = n - row * p.Z;
+    const uint32_t x = p.divY.div(row);
+    const uint32_t y = row - x * p.Y;
+    Nbr c;
+    c.set(x, y, z, p);
+
+    uint8_t fl = 0;
+    uint32_t nsbits = 0;
+    if (MASKED) {
+        fl = p.flags[n];
+        if ((fl & LGB_FLAG_NO_STREAM) && p.nsb) nsbits = p.nsb[n];
+    }
+    R f[S::Q];
+    load_cell<S, Sto, LOAD, MASKED>(p, fin, c, n, nsbits, f);
+
+    if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
+        if constexpr (MASKED) {
+            // a cell runs the substep its index names, and the outlet
+            // substep if it lies on the outlet plane, in sequence order
+            const int idx = fl & LGB_FLAG_INDEX_MASK;
+            const bool outlet = p.abb_k >= 0 && coord_along(c, p.abb_axis) == p.abb_plane;
+            const int outlet_phase = p.abb_k < idx ? 0 : 1;
+#pragma unroll 1
+            for (int phase = 0; phase < 2; ++phase) {
+                if (phase != outlet_phase && idx != p.abb_k)
+                    apply_local_substep<S, COLL>(p, select_sub(p, idx), c, f);
+                if (phase == outlet_phase && outlet)
+                    apply_outlet<S, COLL, LOAD, MASKED, Sto>(p, fin, c, f);
+            }
+        } else {
+            R r;
+            collide<COLL, S>(f, p.cp, r);
+        }
+    }
+
+    if (p.status) {
+        R r = R(0);
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) r += f[q];
+        if (!isfinite(r)) atomicOr(p.status, 1u);
+    }
+
+    const size_t N = p.N;
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        if constexpr (PAT == LGB_PULL || PAT == LGB_LOCAL || PAT == LGB_STREAM_ONLY ||
+                      PAT == LGB_AA_UNPACK) {
+            Sto::store(fout + (size_t)q * N + n, f[q], S::w(q));
+        } else if constexpr (PAT == LGB_AA_EVEN) {
+            Sto::store(fout + (size_t)S::opp(q) * N + n, f[q], S::w(q));
+        } else {  // PUSH, AA_ODD: to the neighbour in direction e_q, slot q
+            const uint32_t dst = c.at(ix<S>(q), iy<S>(q), iz<S>(q), p);
+            if (MASKED && PAT == LGB_PUSH && p.has_nsm && q != 0) {
+                // lettuce keeps the destination's own value where its
+                // no-streaming bit is set
+                const uint8_t fd = p.flags[dst];
+                const bool blocked = (fd & LGB_FLAG_NO_STREAM) && ((p.nsb[dst] >> q) & 1u);
+                if (!blocked) Sto::store(fout + (size_t)q * N + dst, f[q], S::w(q));
+                if ((nsbits >> q) & 1u) Sto::store(fout + (size_t)q * N + n, f[q], S::w(q));
+            } else {
+                Sto::store(fout + (size_t)q * N + dst, f[q], S::w(q));
+            }
+        }
+    }
+}
+
+template <int SID, int ST, int COLL, int PAT, bool MASKED>
+cudaError_t launch_step(const StepParams &p, cudaStream_t stream) {
+    const unsigned threads = 256;
+    const unsigned blocks = (unsigned)((p.N + threads - 1) / threads);
+    step_kernel<SID, ST, COLL, PAT, MASKED><<<blocks, threads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+// collision kinds that are instantiated for a stencil
+template <int SID> constexpr bool has_kbc() { return SID == LGB_D2Q9 || SID == LGB_D3Q27; }
+
+template <int SID, int ST, int PAT, bool MASKED>
+cudaError_t dispatch_collision(int coll, const StepParams &p, cudaStream_t s) {
+    if constexpr (PAT == LGB_STREAM_ONLY || PAT == LGB_AA_UNPACK) {
+        return launch_step<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+    } else {
+    switch (coll) {
+    case LGB_NO_COLLISION: return launch_step<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+    case LGB_BGK: return launch_step<SID, ST, LGB_BGK, PAT, MASKED>(p, s);
+    case LGB_TRT: return launch_step<SID, ST, LGB_TRT, PAT, MASKED>(p, s);
+    case LGB_KBC:
+        if constexpr (has_kbc<SID>()) return launch_step<SID, ST, LGB_KBC, PAT, MASKED>(p, s);
+        return cudaErrorNotSupported;
+    }
+    return cudaErrorInvalidValue;
+    }
+}
+
+template <int SID, int ST, bool MASKED>
+cudaError_t dispatch_pattern(int coll, int pat, const StepParams &p, cudaStream_t s) {
+    switch (pat) {
+    case LGB_PULL: return dispatch_collision<SID, ST, LGB_PULL, MASKED>(coll, p, s);
+    case LGB_PUSH: return dispatch_collision<SID, ST, LGB_PUSH, MASKED>(coll, p, s);
+    case LGB_LOCAL: return dispatch_collision<SID, ST, LGB_LOCAL, MASKED>(coll, p, s);
+    case LGB_AA_EVEN: return dispatch_collision<SID, ST, LGB_AA_EVEN, MASKED>(coll, p, s);
+    case LGB_AA_ODD: return dispatch_collision<SID, ST, LGB_AA_ODD, MASKED>(coll, p, s);
+    case LGB_STREAM_ONLY: return dispatch_collision<SID, ST, LGB_STREAM_ONLY, MASKED>(coll, p, s);
+    case LGB_AA_UNPACK:
+        if constexpr (!MASKED) return dispatch_collision<SID, ST, LGB_AA_UNPACK, false>(coll, p, s);
+        return cudaErrorInvalidValue;
+    }
+    return cudaErrorInvalidValue;
+}
+
+// one translation unit per (stencil, storage): lgb_step_<stencil>.cu built
+// with -DLGB_STORAGE_ID=<storage>
+#define LGB_DECLARE_STEP(name)                                                              \
+    cudaError_t name##_s0(int, int, bool, const StepParams &, cudaStream_t);              \
+    cudaError_t name##_s1(int, int, bool, const StepParams &, cudaStream_t);              \
+    cudaError_t name##_s2(int, int, bool, const StepParams &, cudaStream_t);              \
+    cudaError_t name##_s3(int, int, bool, const StepParams &, cudaStream_t);
+LGB_DECLARE_STEP(step_d1q3)
+LGB_DECLARE_STEP(step_d2q9)
+LGB_DECLARE_STEP(step_d3q15)
+LGB_DECLARE_STEP(step_d3q19)
+LGB_DECLARE_STEP(step_d3q27)
+#undef LGB_DECLARE_STEP
+
+}  // namespace lgb

@@ -1,0 +1,18 @@
+// Instantiations of the generic step kernel for D3Q27; compiled once per
+// population storage (-DLGB_STORAGE_ID=0..3) so the build runs them in
+// parallel.
+#include "lgb_step.cuh"
+
+#ifndef LGB_STORAGE_ID
+#error "compile with -DLGB_STORAGE_ID=<storage>"
+#endif
+#define LGB_CAT2(a, b) a##b
+#define LGB_CAT(a, b) LGB_CAT2(a, b)
+
+namespace lgb {
+cudaError_t LGB_CAT(step_d3q27_s, LGB_STORAGE_ID)(int coll, int pat, bool masked,
+                                                  const StepParams &p, cudaStream_t s) {
+    return masked ? dispatch_pattern<LGB_D3Q27, LGB_STORAGE_ID, true>(coll, pat, p, s)
+                  : dispatch_pattern<LGB_D3Q27, LGB_STORAGE_ID, false>(coll, pat, p, s);
+}
+}  // namespace lgb

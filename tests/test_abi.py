@@ -1,0 +1,129 @@
+"""The C ABI library without a GPU: it loads, exports every function the
+public header declares, its struct layouts match the header as compiled by
+a C compiler, and argument validation fails cleanly (these errors are
+raised before any CUDA call)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "lettuce_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(lgb_\w+)\s*\(", text, re.M)))
+
+
+def test_exports_every_declared_symbol(lgb):
+    from lettuce_gb300 import _lib
+    L = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 7
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(_lib.EXPORTED)
+    assert L.lgb_abi_version() == _lib.ABI_VERSION
+    assert L.lgb_reduce_scratch_bytes() > 0
+
+
+def test_struct_layout_matches_header(tmp_path, lgb):
+    from lettuce_gb300 import _lib
+    src = tmp_path / "probe.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "lettuce_gb300.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(lgb_step_desc),"
+        " offsetof(lgb_step_desc, sub), offsetof(lgb_step_desc, status),"
+        " sizeof(lgb_substep), offsetof(lgb_substep, rho), offsetof(lgb_substep, u_stride));"
+        "return 0;}\n")
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    S, D = _lib.Substep, _lib.StepDesc
+    assert got == [ctypes.sizeof(D), D.sub.offset, D.status.offset, ctypes.sizeof(S),
+                   S.rho.offset, S.u_stride.offset]
+
+
+def _desc(**kw):
+    from lettuce_gb300 import _device, _lib
+    d = _device.new_desc(kw.pop("stencil", _lib.D2Q9), kw.pop("storage", _lib.F32),
+                         kw.pop("res", [8, 8]))
+    d.collision = _lib.BGK
+    d.tau = 0.6
+    d.f_in = 0x1000
+    d.f_out = 0x2000
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(abi_version=99), "ABI version"),
+    (dict(stencil=7), "unknown stencil"),
+    (dict(storage=9), "unknown storage"),
+    (dict(collision=3, stencil=4, res=[4, 4, 4]), "KBC collision is only defined"),
+    (dict(pattern=42), "unknown access pattern"),
+    (dict(f_out=0x1000), "distinct input and output"),
+    (dict(tau=0.0), "relaxation time must be positive"),
+    (dict(res=[0, 8]), "must be positive"),
+    (dict(res=[70000, 70000]), "exceeds"),
+    (dict(f_in=0), "NULL"),
+])
+def test_step_validation_errors(lgb, kw, msg):
+    from lettuce_gb300 import _lib
+    L = _lib.load()
+    d = _desc(**kw)
+    rc = L.lgb_step(ctypes.byref(d), None)
+    assert rc != 0
+    assert msg in L.lgb_last_error().decode()
+
+
+def test_step_validation_masked(lgb):
+    from lettuce_gb300 import _lib
+    L = _lib.load()
+    d = _desc(flags=0x3000, n_sub=2, collision_index=0)
+    d.sub[0].kind = _lib.SUB_COLLISION
+    d.sub[1].kind = _lib.SUB_EQUILIBRIUM_PU  # without rho/u
+    assert L.lgb_step(ctypes.byref(d), None) != 0
+    assert "lacks rho/u" in L.lgb_last_error().decode()
+    d = _desc(flags=0x3000, n_sub=3, collision_index=0, no_stream_bits=0x4000,
+              pattern=_lib.AA_EVEN)
+    d.sub[0].kind = _lib.SUB_COLLISION
+    d.sub[1].kind = _lib.SUB_BOUNCE_BACK
+    d.sub[2].kind = _lib.SUB_ANTI_BOUNCE_BACK
+    d.sub[2].sign = 1
+    assert L.lgb_step(ctypes.byref(d), None) != 0
+    assert "AA pattern" in L.lgb_last_error().decode()
+    d = _desc(flags=0x3000, n_sub=3, collision_index=1)
+    d.sub[0].kind = _lib.SUB_BOUNCE_BACK
+    d.sub[1].kind = _lib.SUB_BOUNCE_BACK
+    assert L.lgb_step(ctypes.byref(d), None) != 0
+    assert "collision_index" in L.lgb_last_error().decode()
+
+
+def test_reduce_and_convert_validation(lgb):
+    from lettuce_gb300 import _lib
+    L = _lib.load()
+    r = _lib.i32x3([8, 8])
+    lo = _lib.i32x3([0, 0])
+    hi = _lib.i32x3([9, 8])
+    rc = L.lgb_reduce(_lib.D2Q9, _lib.F32, ctypes.cast(r, ctypes.c_void_p), 0x1000, 0,
+                      ctypes.cast(lo, ctypes.c_void_p), ctypes.cast(hi, ctypes.c_void_p),
+                      None, 0x2000, 0x3000, None)
+    assert rc != 0 and "box" in L.lgb_last_error().decode()
+    assert L.lgb_convert(_lib.D2Q9, 5, 0x1000, _lib.F32, 0x2000, 10, None) != 0
+    assert L.lgb_convert(_lib.D2Q9, _lib.F32, 0x1000, _lib.F32, 0x2000, 0, None) == 0
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from lettuce_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "library_path", lambda: str(tmp_path / "nope.so"))
+    with pytest.raises(_lib.LibraryError, match="no fallback"):
+        _lib.load()

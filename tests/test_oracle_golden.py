@@ -1,0 +1,103 @@
+"""Pins the CPU oracle to lettuce: every golden vector in tests/golden was
+produced by lettuce's own float64 torch step (tests/golden/make_golden.py);
+the oracle must reproduce each to float64 round-off."""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_names, meta
+
+STRATS = ["PRE_STREAMING", "POST_STREAMING"]
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(1e-300, np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("name", golden_names("random_") + golden_names("tgv2d_d2q9")
+                         + golden_names("tgv3d"))
+@pytest.mark.parametrize("strategy", STRATS)
+def test_periodic_cases(oracle, name, strategy):
+    z = golden(name)
+    m = meta(z)
+    out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision=m["collision"],
+                     tau=float(z["tau"]), tau_minus=1.0, strategy=strategy)
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+def obstacle_boundaries(z, m):
+    res = m["res"]
+    d = len(res)
+    x = np.arange(res[0]).reshape([-1] + [1] * (d - 1)) * np.ones(res)
+    return [{"kind": "equilibrium_pu", "mask": np.abs(x) < 1e-6,
+             "rho": z["inlet_rho_lu"].reshape([1] * d),
+             "u": z["inlet_u_lu"].reshape([d] + [1] * d)},
+            {"kind": "anti_bounce_back", "direction": [1] + [0] * (d - 1)},
+            {"kind": "bounce_back", "mask": z["mask"]}]
+
+
+@pytest.mark.parametrize("name", golden_names("obstacle"))
+def test_obstacle_masks_bit_exact(oracle, name):
+    z = golden(name)
+    m = meta(z)
+    ncm, nsm = oracle.assemble_masks(m["res"], z["f0"].shape[0], m["stencil"], [],
+                                     obstacle_boundaries(z, m))
+    assert np.array_equal(ncm, z["ncm"])
+    assert np.array_equal(nsm, z["nsm"])
+
+
+@pytest.mark.parametrize("name", golden_names("obstacle"))
+@pytest.mark.parametrize("strategy", STRATS)
+def test_obstacle_cases(oracle, name, strategy):
+    z = golden(name)
+    m = meta(z)
+    out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision=m["collision"],
+                     tau=float(z["tau"]), strategy=strategy,
+                     post=obstacle_boundaries(z, m))
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+def test_equilibrium_boundary_field(oracle, strategy):
+    z = golden("eqpu_field_d2q9")
+    post = [{"kind": "equilibrium_pu", "mask": z["mask"], "rho": z["rho_lu"][0],
+             "u": z["u_lu"]}]
+    out = oracle.run("D2Q9", z["f0"], int(z["steps"]), collision="bgk",
+                     tau=float(z["tau"]), strategy=strategy, post=post)
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+def test_native_known_answers(oracle):
+    """lettuce tests/native/test_native_streaming.py (impulse per direction)
+    and test_native_bounce_back.py"""
+    z = golden("native_kats")
+    out = oracle.run("D2Q9", z["stream_f0"], 1, collision="none")
+    assert np.array_equal(out, z["stream_f1"])
+    post = [{"kind": "bounce_back", "mask": z["bb_mask"]}]
+    assert np.array_equal(oracle.run("D2Q9", z["bb_f0"], 1, collision="none", post=post),
+                          z["bb_f1"])
+    assert np.array_equal(oracle.run("D2Q9", z["bb_f0"], 2, collision="none", post=post),
+                          z["bb_f2"])
+
+
+def test_oracle_moments_match_golden(oracle):
+    z = golden("observables")
+    rho, u = oracle.moments("D2Q9", z["2d_f"])
+    assert np.allclose(rho, z["2d_rho"][0], rtol=1e-14, atol=0)
+    assert np.allclose(u, z["2d_u"], rtol=1e-12, atol=1e-16)
+
+
+def test_oracle_energy_decay_series(oracle):
+    """config 1: D2Q9 BGK TGV 256^2, Re 1000, f64, POST_STREAMING; the oracle
+    must follow lettuce's kinetic energy series (first 100 steps here)"""
+    z = golden("observables")  # noqa: F841  (units checked in test_host)
+    e = golden("tgv2d_energy_256")
+    import lettuce_gb300 as lt
+    import torch
+    ctx = lt.Context("cpu", torch.float64)
+    flow = lt.TaylorGreenVortex(ctx, 256, 1000, 0.05, lt.D2Q9)
+    f0 = flow.f.numpy()
+    tau = flow.units.relaxation_parameter_lu
+    f100 = oracle.run("D2Q9", f0, 100, collision="bgk", tau=tau, strategy="POST_STREAMING")
+    dx = flow.units.convert_length_to_pu(1.0)
+    k = flow.units.convert_incompressible_energy_to_pu(oracle.kinetic_energy("D2Q9", f100))
+    assert abs(k * dx ** 2 / e["energy"][1] - 1) < 1e-12
