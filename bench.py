@@ -285,8 +285,11 @@ def run_ours(args, world, rank, local):
 
     variants = {}
     clocks = None
+    wanted = set(args.variants.split(","))
     for key, storage, pattern in [("f32_pull", None, "pull"), ("f16s_pull", "fp16_shifted", "pull"),
                                   ("f32_aa", None, "aa"), ("f16s_aa", "fp16_shifted", "aa")]:
+        if key not in wanted:
+            continue
         barrier(world)
         if key == "f32_pull":
             with ClockSampler(local) as cs:
@@ -306,6 +309,9 @@ def run_ours(args, world, rank, local):
         del flow, sim
         torch.cuda.empty_cache()
 
+    if args.profile_only:
+        print(json.dumps({"variants": variants, "grid": RES}), flush=True)
+        return 0
     head = variants["f32_pull"]
     ms = head["ms_per_step"]
     achieved = head["achieved_gbs"]
@@ -349,7 +355,7 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         return 0
-    f16 = variants["f16s_pull"]
+    f16 = variants.get("f16s_pull", {"mlups": 0.0, "frac_of_peak": None, "achieved_gbs": None})
     line = {
         "metric": METRIC, "value": head["mlups"], "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -392,7 +398,16 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--grid", type=int, default=256,
+                    help="cube side (profiling a smaller case; the benchmark is 256)")
+    ap.add_argument("--variants", default="f32_pull,f16s_pull,f32_aa,f16s_aa")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="time the selected variants only and print them")
     args = ap.parse_args()
+    global RES
+    RES = [args.grid] * 3
+    if not args.profile_only and "f32_pull" not in args.variants:
+        ap.error("the benchmark line needs the f32_pull variant")
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup(args)

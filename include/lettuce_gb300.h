@@ -94,7 +94,13 @@ typedef struct {
     int32_t collision_index;
     lgb_substep sub[LGB_MAX_SUBSTEPS];
     uint32_t *status;        /* optional device word; bit 0 set on a non-finite density */
+    int32_t options;         /* LGB_OPT_* bits */
+    int32_t reserved;
 } lgb_step_desc;
+
+/* options: run the one-cell-per-thread kernel even where the two-cell
+ * kernel of the 16-bit formats applies (results are bit-identical) */
+#define LGB_OPT_ONE_CELL 1
 
 /* ABI version of the loaded library */
 int lgb_abi_version(void);

@@ -23,6 +23,7 @@ NO_COLLISION, BGK, TRT, KBC = 0, 1, 2, 3
 SUB_COLLISION, SUB_BOUNCE_BACK, SUB_EQUILIBRIUM_PU, SUB_ANTI_BOUNCE_BACK, SUB_NONE = 0, 1, 2, 3, 4
 PULL, PUSH, LOCAL, AA_EVEN, AA_ODD, STREAM_ONLY, AA_UNPACK = 0, 1, 2, 3, 4, 5, 6
 FLAG_INDEX_MASK, FLAG_NO_STREAM = 0x1F, 0x80
+OPT_ONE_CELL = 1
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
             "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_convert"]
@@ -55,7 +56,9 @@ class StepDesc(ctypes.Structure):
                 ("n_sub", ctypes.c_int32),
                 ("collision_index", ctypes.c_int32),
                 ("sub", Substep * MAX_SUBSTEPS),
-                ("status", ctypes.c_void_p)]
+                ("status", ctypes.c_void_p),
+                ("options", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class LibraryError(RuntimeError):

@@ -12,6 +12,7 @@
 
 #include "lettuce_gb300.h"
 #include "lgb_step.cuh"
+#include "lgb_step_vec.cuh"
 
 namespace {
 
@@ -83,6 +84,31 @@ cudaError_t dispatch_step(int stencil, int storage, int coll, int pat, bool mask
     case LGB_D3Q27: LGB_STORAGE_SWITCH(step_d3q27)
     }
 #undef LGB_STORAGE_SWITCH
+    return cudaErrorInvalidValue;
+}
+
+// the two-cell kernel of the 16-bit storages: no boundaries, BGK / TRT /
+// no collision, an even row length and one of its five patterns
+bool use_vec2(int storage, int coll, int pat, bool masked, uint32_t Z) {
+    return (storage == LGB_F16_SHIFTED || storage == LGB_BF16_SHIFTED) && !masked &&
+           (coll == LGB_NO_COLLISION || coll == LGB_BGK || coll == LGB_TRT) && Z % 2 == 0 &&
+           (pat == LGB_PULL || pat == LGB_PUSH || pat == LGB_LOCAL || pat == LGB_AA_EVEN ||
+            pat == LGB_AA_ODD);
+}
+
+cudaError_t dispatch_step_vec2(int stencil, int storage, int coll, int pat,
+                               const lgb::StepParams &p, cudaStream_t s) {
+#define LGB_VEC_SWITCH(name)                                                \
+    return storage == LGB_F16_SHIFTED ? lgb::name##_s2(coll, pat, p, s)     \
+                                      : lgb::name##_s3(coll, pat, p, s);
+    switch (stencil) {
+    case LGB_D1Q3: LGB_VEC_SWITCH(step_vec2_d1q3)
+    case LGB_D2Q9: LGB_VEC_SWITCH(step_vec2_d2q9)
+    case LGB_D3Q15: LGB_VEC_SWITCH(step_vec2_d3q15)
+    case LGB_D3Q19: LGB_VEC_SWITCH(step_vec2_d3q19)
+    case LGB_D3Q27: LGB_VEC_SWITCH(step_vec2_d3q27)
+    }
+#undef LGB_VEC_SWITCH
     return cudaErrorInvalidValue;
 }
 
@@ -431,8 +457,13 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (p.abb_k >= 0 && d->f_in == d->f_out)
         return fail("lgb_step: the anti-bounce-back outlet reads its neighbour plane and "
                     "needs distinct input and output fields");
-    cudaError_t e = dispatch_step(d->stencil, d->storage, d->collision, d->pattern, masked, p,
-                                  static_cast<cudaStream_t>(stream));
+    const bool vec2 = !(d->options & LGB_OPT_ONE_CELL) &&
+                      use_vec2(d->storage, d->collision, d->pattern, masked, g.Z);
+    cudaError_t e = vec2
+                        ? dispatch_step_vec2(d->stencil, d->storage, d->collision, d->pattern, p,
+                                             static_cast<cudaStream_t>(stream))
+                        : dispatch_step(d->stencil, d->storage, d->collision, d->pattern, masked,
+                                        p, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "lgb_step: launch failed");
     return 0;
 }

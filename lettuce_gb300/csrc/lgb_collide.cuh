@@ -15,7 +15,7 @@
 namespace lgb {
 
 template <class S, class R>
-__device__ __forceinline__ void cell_moments(const R (&f)[S::Q], R &rho, R (&u)[3]) {
+LGB_HD void cell_moments(const R (&f)[S::Q], R &rho, R (&u)[3]) {
     R r = R(0);
 #pragma unroll
     for (int q = 0; q < S::Q; ++q) r += f[q];
@@ -39,7 +39,7 @@ __device__ __forceinline__ void cell_moments(const R (&f)[S::Q], R &rho, R (&u)[
 }
 
 template <class S, class R>
-__device__ __forceinline__ R feq_q(int q, R rho, const R (&u)[3], R uu) {
+LGB_HD R feq_q(int q, R rho, const R (&u)[3], R uu) {
     R eu = R(0);
 #pragma unroll
     for (int d = 0; d < S::D; ++d) {
@@ -52,7 +52,7 @@ __device__ __forceinline__ R feq_q(int q, R rho, const R (&u)[3], R uu) {
 }
 
 template <class S, class R>
-__device__ __forceinline__ R dot_uu(const R (&u)[3]) {
+LGB_HD R dot_uu(const R (&u)[3]) {
     R uu = R(0);
 #pragma unroll
     for (int d = 0; d < S::D; ++d) uu += u[d] * u[d];
@@ -60,7 +60,7 @@ __device__ __forceinline__ R dot_uu(const R (&u)[3]) {
 }
 
 template <class S, class R>
-__device__ __forceinline__ void set_equilibrium(R (&f)[S::Q], R rho, const R (&u)[3]) {
+LGB_HD void set_equilibrium(R (&f)[S::Q], R rho, const R (&u)[3]) {
     const R uu = dot_uu<S>(u);
 #pragma unroll
     for (int q = 0; q < S::Q; ++q) f[q] = feq_q<S>(q, rho, u, uu);
@@ -74,7 +74,7 @@ struct CollideParams {
 };
 
 template <class S, class R>
-__device__ __forceinline__ void collide_bgk(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+LGB_HD void collide_bgk(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     R rho, u[3];
     cell_moments<S>(f, rho, u);
     const R uu = dot_uu<S>(u);
@@ -85,7 +85,7 @@ __device__ __forceinline__ void collide_bgk(R (&f)[S::Q], const CollideParams &c
 }
 
 template <class S, class R>
-__device__ __forceinline__ void collide_trt(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+LGB_HD void collide_trt(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     R rho, u[3];
     cell_moments<S>(f, rho, u);
     const R uu = dot_uu<S>(u);
@@ -108,7 +108,7 @@ __device__ __forceinline__ void collide_trt(R (&f)[S::Q], const CollideParams &c
 // moment transform of kbc_collision.py:25-39 restricted to the second
 // moments it consumes, and compute_s_seq_from_m_{3d,2d} (:44-94).
 template <class S, class R>
-__device__ __forceinline__ void kbc_shear(const R (&g)[S::Q], R rho_g, R (&s)[S::Q]) {
+LGB_HD void kbc_shear(const R (&g)[S::Q], R rho_g, R (&s)[S::Q]) {
     static_assert(S::Q == 27 || S::Q == 9, "KBC is defined for D3Q27 and D2Q9");
     if constexpr (S::Q == 27) {
         R mxx = 0, myy = 0, mzz = 0, mxy = 0, mxz = 0, myz = 0;
@@ -159,7 +159,7 @@ __device__ __forceinline__ void kbc_shear(const R (&g)[S::Q], R rho_g, R (&s)[S:
 }
 
 template <class S, class R>
-__device__ __forceinline__ void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     R rho, u[3];
     cell_moments<S>(f, rho, u);
     const R uu = dot_uu<S>(u);
@@ -191,7 +191,7 @@ __device__ __forceinline__ void collide_kbc(R (&f)[S::Q], const CollideParams &c
 }
 
 template <int COLL, class S, class R>
-__device__ __forceinline__ void collide(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+LGB_HD void collide(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     if constexpr (COLL == LGB_BGK) {
         collide_bgk<S>(f, cp, rho_out);
     } else if constexpr (COLL == LGB_TRT) {

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "lgb_collide.cuh"
+#include "lgb_shifted.cuh"
 #include "lgb_storage.cuh"
 
 namespace lgb {
@@ -98,7 +99,7 @@ template <> struct PatternTraits<LGB_AA_ODD> { static constexpr int load = LOAD_
 template <> struct PatternTraits<LGB_AA_UNPACK> { static constexpr int load = LOAD_AA_ODD; };
 
 // populations of the cell `c` (index n) as the collide phase sees them
-template <class S, class Sto, int LOAD, bool MASKED>
+template <class S, class Sto, int LOAD, bool MASKED, bool RAW = false>
 __device__ __forceinline__ void load_cell(const StepParams &p, const typename Sto::T *__restrict__ fin,
                                           const Nbr &c, uint32_t n, uint32_t nsbits,
                                           typename Sto::R (&f)[S::Q]) {
@@ -112,7 +113,8 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
             if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
             if (MASKED && LOAD == LOAD_PULL && q != 0 && ((nsbits >> q) & 1u)) src = n;
         }
-        f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
+        if constexpr (RAW) f[q] = Sto::load_h(fin + (size_t)slot * N + src);
+        else f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
     }
 }
 
@@ -211,6 +213,12 @@ __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename
     }
 }
 
+template <class Sto, bool RAW>
+__device__ __forceinline__ void store_value(typename Sto::T *ptr, typename Sto::R v, double w) {
+    if constexpr (RAW) Sto::store_h(ptr, v);
+    else Sto::store(ptr, v, w);
+}
+
 template <int SID, int ST, int COLL, int PAT, bool MASKED>
 __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     using S = Stencil<SID>;
@@ -218,6 +226,9 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     using R = typename Sto::R;
     using T = typename Sto::T;
     constexpr int LOAD = PatternTraits<PAT>::load;
+    // 16-bit formats without boundaries collide in shifted space, with the
+    // same arithmetic as the two-cell kernel
+    constexpr bool HSPACE = is_shifted<ST>() && !MASKED && shifted_collision<COLL>();
     const T *__restrict__ fin = static_cast<const T *>(p.f_in);
     T *fout = static_cast<T *>(p.f_out);
     const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -236,9 +247,12 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
         if ((fl & LGB_FLAG_NO_STREAM) && p.nsb) nsbits = p.nsb[n];
     }
     R f[S::Q];
-    load_cell<S, Sto, LOAD, MASKED>(p, fin, c, n, nsbits, f);
+    load_cell<S, Sto, LOAD, MASKED, HSPACE>(p, fin, c, n, nsbits, f);
 
-    if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
+    if constexpr (HSPACE) {
+        if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK)
+            collide_shifted<S, Lane1, COLL>(f, p.cp);
+    } else if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
         if constexpr (MASKED) {
             // a cell runs the substep its index names, and the outlet
             // substep if it lies on the outlet plane, in sequence order
@@ -270,9 +284,9 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     for (int q = 0; q < S::Q; ++q) {
         if constexpr (PAT == LGB_PULL || PAT == LGB_LOCAL || PAT == LGB_STREAM_ONLY ||
                       PAT == LGB_AA_UNPACK) {
-            Sto::store(fout + (size_t)q * N + n, f[q], S::w(q));
+            store_value<Sto, HSPACE>(fout + (size_t)q * N + n, f[q], S::w(q));
         } else if constexpr (PAT == LGB_AA_EVEN) {
-            Sto::store(fout + (size_t)S::opp(q) * N + n, f[q], S::w(q));
+            store_value<Sto, HSPACE>(fout + (size_t)S::opp(q) * N + n, f[q], S::w(q));
         } else {  // PUSH, AA_ODD: to the neighbour in direction e_q, slot q
             const uint32_t dst = c.at(ix<S>(q), iy<S>(q), iz<S>(q), p);
             if (MASKED && PAT == LGB_PUSH && p.has_nsm && q != 0) {
@@ -280,10 +294,10 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
                 // no-streaming bit is set
                 const uint8_t fd = p.flags[dst];
                 const bool blocked = (fd & LGB_FLAG_NO_STREAM) && ((p.nsb[dst] >> q) & 1u);
-                if (!blocked) Sto::store(fout + (size_t)q * N + dst, f[q], S::w(q));
-                if ((nsbits >> q) & 1u) Sto::store(fout + (size_t)q * N + n, f[q], S::w(q));
+                if (!blocked) store_value<Sto, HSPACE>(fout + (size_t)q * N + dst, f[q], S::w(q));
+                if ((nsbits >> q) & 1u) store_value<Sto, HSPACE>(fout + (size_t)q * N + n, f[q], S::w(q));
             } else {
-                Sto::store(fout + (size_t)q * N + dst, f[q], S::w(q));
+                store_value<Sto, HSPACE>(fout + (size_t)q * N + dst, f[q], S::w(q));
             }
         }
     }

@@ -1,0 +1,163 @@
+// Two cells per thread for the shifted 16-bit population formats on grids
+// without boundaries: every population of a cell pair is one 32-bit word
+// (a half2 / bfloat162) of the row, so loads and stores are full-width and
+// coalesced. A shift of the pair by one cell along the contiguous axis (the
+// z component of e_q) straddles two words: both aligned words are loaded
+// and one byte permute extracts the shifted pair (row ends wrap
+// periodically). The collision runs on both cells at once with the packed
+// f32x2 instructions (lgb_shifted.cuh), bit-identical to the one-cell path.
+//
+// Patterns: PULL, PUSH, LOCAL, AA_EVEN, AA_ODD. PUSH and AA_ODD store a
+// shifted pair as two 16-bit stores (each half is written by exactly one
+// thread, so there is no race).
+#pragma once
+
+#include "lgb_shifted.cuh"
+#include "lgb_step.cuh"
+
+namespace lgb {
+
+template <int ST> struct Pack16;
+template <> struct Pack16<LGB_F16_SHIFTED> {
+    static __device__ __forceinline__ float2 decode(uint32_t w) {
+        __half2 h = *reinterpret_cast<__half2 *>(&w);
+        return __half22float2(h);
+    }
+    static __device__ __forceinline__ uint32_t encode(float2 v) {
+        __half2 h = __float22half2_rn(v);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+};
+template <> struct Pack16<LGB_BF16_SHIFTED> {
+    static __device__ __forceinline__ float2 decode(uint32_t w) {
+        __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&w);
+        return __bfloat1622float2(h);
+    }
+    static __device__ __forceinline__ uint32_t encode(float2 v) {
+        __nv_bfloat162 h = __float22bfloat162_rn(v);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+};
+
+// the pair (z0 + dz, z0 + 1 + dz) of a row, dz in {-1, 0, 1}, from the
+// aligned words at pair index tz and its periodic neighbours
+__device__ __forceinline__ uint32_t load_pair(const uint32_t *__restrict__ row, uint32_t tz,
+                                              uint32_t tzm, uint32_t tzp, int dz) {
+    if (dz == 0) return __ldg(row + tz);
+    if (dz < 0) return __byte_perm(__ldg(row + tzm), __ldg(row + tz), 0x5432);
+    return __byte_perm(__ldg(row + tz), __ldg(row + tzp), 0x5432);
+}
+
+template <int SID, int ST, int COLL, int PAT>
+__global__ void __launch_bounds__(256) step_vec2_kernel(const StepParams p) {
+    using S = Stencil<SID>;
+    using P = Pack16<ST>;
+    const uint32_t Zh = p.Z >> 1;
+    const uint32_t Nh = p.N >> 1;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Nh) return;
+    const uint32_t row = p.divZ.div(t);  // divZ holds Z/2 here
+    const uint32_t tz = t - row * Zh;
+    const uint32_t x = p.divY.div(row);
+    const uint32_t y = row - x * p.Y;
+    const uint32_t xm = x == 0 ? p.X - 1 : x - 1, xp = x + 1 == p.X ? 0 : x + 1;
+    const uint32_t ym = y == 0 ? p.Y - 1 : y - 1, yp = y + 1 == p.Y ? 0 : y + 1;
+    const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
+    const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in);
+    auto row_of = [&](int dx, int dy) -> uint32_t {
+        const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
+        const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
+        return (a * p.Y + b) * Zh;
+    };
+
+    float2 h[S::Q];
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        uint32_t w;
+        if constexpr (PAT == LGB_PULL || PAT == LGB_AA_ODD) {
+            const int slot = PAT == LGB_AA_ODD ? S::opp(q) : q;
+            const uint32_t *r = fin + (size_t)slot * Nh + row_of(-ix<S>(q), -iy<S>(q));
+            w = load_pair(r, tz, tzm, tzp, -iz<S>(q));
+        } else {
+            w = __ldg(fin + (size_t)q * Nh + row * Zh + tz);
+        }
+        h[q] = P::decode(w);
+    }
+
+    collide_shifted<S, Lane2, COLL>(h, p.cp);
+
+    if (p.status) {
+        float2 r = h[0];
+#pragma unroll
+        for (int q = 1; q < S::Q; ++q) r = Lane2::add(r, h[q]);
+        if (!isfinite(r.x) || !isfinite(r.y)) atomicOr(p.status, 1u);
+    }
+
+    uint32_t *fout = static_cast<uint32_t *>(p.f_out);
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        const uint32_t w = P::encode(h[q]);
+        if constexpr (PAT == LGB_PULL || PAT == LGB_LOCAL) {
+            fout[(size_t)q * Nh + row * Zh + tz] = w;
+        } else if constexpr (PAT == LGB_AA_EVEN) {
+            fout[(size_t)S::opp(q) * Nh + row * Zh + tz] = w;
+        } else {  // PUSH, AA_ODD: to (x, y, z) + e_q, slot q
+            uint32_t *r = fout + (size_t)q * Nh + row_of(ix<S>(q), iy<S>(q));
+            const int dz = iz<S>(q);
+            if (dz == 0) {
+                r[tz] = w;
+            } else {
+                unsigned short *r16 = reinterpret_cast<unsigned short *>(r);
+                const uint32_t z0 = 2 * tz;
+                const uint32_t za = dz > 0 ? z0 + 1 : (z0 == 0 ? p.Z - 1 : z0 - 1);
+                const uint32_t zb = dz > 0 ? (z0 + 2 == p.Z ? 0 : z0 + 2) : z0;
+                r16[za] = (unsigned short)(w & 0xffffu);
+                r16[zb] = (unsigned short)(w >> 16);
+            }
+        }
+    }
+}
+
+template <int SID, int ST, int COLL, int PAT>
+cudaError_t launch_step_vec2(const StepParams &p0, cudaStream_t stream) {
+    StepParams p = p0;
+    p.divZ = FastDiv::make(p.Z >> 1);
+    const unsigned threads = 256;
+    const unsigned blocks = (unsigned)(((p.N >> 1) + threads - 1) / threads);
+    step_vec2_kernel<SID, ST, COLL, PAT><<<blocks, threads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <int SID, int ST, int PAT>
+cudaError_t dispatch_vec2_collision(int coll, const StepParams &p, cudaStream_t s) {
+    switch (coll) {
+    case LGB_NO_COLLISION: return launch_step_vec2<SID, ST, LGB_NO_COLLISION, PAT>(p, s);
+    case LGB_BGK: return launch_step_vec2<SID, ST, LGB_BGK, PAT>(p, s);
+    case LGB_TRT: return launch_step_vec2<SID, ST, LGB_TRT, PAT>(p, s);
+    }
+    return cudaErrorNotSupported;
+}
+
+template <int SID, int ST>
+cudaError_t dispatch_vec2(int coll, int pat, const StepParams &p, cudaStream_t s) {
+    switch (pat) {
+    case LGB_PULL: return dispatch_vec2_collision<SID, ST, LGB_PULL>(coll, p, s);
+    case LGB_PUSH: return dispatch_vec2_collision<SID, ST, LGB_PUSH>(coll, p, s);
+    case LGB_LOCAL: return dispatch_vec2_collision<SID, ST, LGB_LOCAL>(coll, p, s);
+    case LGB_AA_EVEN: return dispatch_vec2_collision<SID, ST, LGB_AA_EVEN>(coll, p, s);
+    case LGB_AA_ODD: return dispatch_vec2_collision<SID, ST, LGB_AA_ODD>(coll, p, s);
+    }
+    return cudaErrorNotSupported;
+}
+
+#define LGB_DECLARE_VEC(name)                                                            \
+    cudaError_t name##_s2(int, int, const StepParams &, cudaStream_t);                    \
+    cudaError_t name##_s3(int, int, const StepParams &, cudaStream_t);
+LGB_DECLARE_VEC(step_vec2_d1q3)
+LGB_DECLARE_VEC(step_vec2_d2q9)
+LGB_DECLARE_VEC(step_vec2_d3q15)
+LGB_DECLARE_VEC(step_vec2_d3q19)
+LGB_DECLARE_VEC(step_vec2_d3q27)
+#undef LGB_DECLARE_VEC
+
+}  // namespace lgb

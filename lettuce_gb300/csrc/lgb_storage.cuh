@@ -49,6 +49,9 @@ template <> struct Storage<LGB_F16_SHIFTED> {
         __stcs(reinterpret_cast<unsigned short *>(p),
                __half_as_ushort(__float2half_rn(v - (float)w)));
     }
+    // the stored deviation h = f - w itself
+    static __device__ __forceinline__ R load_h(const T *p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void store_h(T *p, R h) { *p = __float2half_rn(h); }
 };
 
 template <> struct Storage<LGB_BF16_SHIFTED> {
@@ -67,7 +70,13 @@ template <> struct Storage<LGB_BF16_SHIFTED> {
         __stcs(reinterpret_cast<unsigned short *>(p),
                __bfloat16_as_ushort(__float2bfloat16_rn(v - (float)w)));
     }
+    static __device__ __forceinline__ R load_h(const T *p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void store_h(T *p, R h) { *p = __float2bfloat16_rn(h); }
 };
+
+template <int ST> __host__ __device__ constexpr bool is_shifted() {
+    return ST == LGB_F16_SHIFTED || ST == LGB_BF16_SHIFTED;
+}
 
 inline int storage_bytes(int st) {
     return st == LGB_F64 ? 8 : (st == LGB_F32 ? 4 : 2);

@@ -37,7 +37,7 @@ def test_struct_layout_matches_header(tmp_path, lgb):
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "lettuce_gb300.h"\n'
         "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(lgb_step_desc),"
-        " offsetof(lgb_step_desc, sub), offsetof(lgb_step_desc, status),"
+        " offsetof(lgb_step_desc, sub), offsetof(lgb_step_desc, options),"
         " sizeof(lgb_substep), offsetof(lgb_substep, rho), offsetof(lgb_substep, u_stride));"
         "return 0;}\n")
     exe = tmp_path / "probe"
@@ -46,7 +46,7 @@ def test_struct_layout_matches_header(tmp_path, lgb):
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
     S, D = _lib.Substep, _lib.StepDesc
-    assert got == [ctypes.sizeof(D), D.sub.offset, D.status.offset, ctypes.sizeof(S),
+    assert got == [ctypes.sizeof(D), D.sub.offset, D.options.offset, ctypes.sizeof(S),
                    S.rho.offset, S.u_stride.offset]
 
 
