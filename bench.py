@@ -241,10 +241,12 @@ def time_variant(lt, torch, storage, pattern, steps, warmup, device):
     torch.cuda.synchronize(device)
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("lgb_timed")
     start.record(stream)
     for _ in range(steps):
         sim._collide_and_stream()
     end.record(stream)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize(device)
     ms = start.elapsed_time(end) / steps
     return ms, flow, sim

@@ -84,6 +84,20 @@ __device__ __forceinline__ typename L::V dot_e_u(int q, const typename L::V (&u)
     return eu;
 }
 
+// weight class of a velocity: |e|^2 (0 rest, 1 axis, 2 face diagonal,
+// 3 space diagonal); every lettuce stencil has one weight per class
+template <class S> __host__ __device__ constexpr int weight_class(int q) {
+    int s = 0;
+    for (int d = 0; d < S::D; ++d) s += S::e(q, d) * S::e(q, d);
+    return s;
+}
+// first velocity of class k, or -1 when the stencil has none
+template <class S> __host__ __device__ constexpr int weight_class_rep(int k) {
+    for (int q = 0; q < S::Q; ++q)
+        if (weight_class<S>(q) == k) return q;
+    return -1;
+}
+
 // shifted equilibria of the pair (q, opposite(q)): they share e.u up to sign
 template <class S, class L>
 __device__ __forceinline__ void shifted_feq_pair(int q, typename L::V drho, typename L::V rho,
@@ -110,20 +124,33 @@ __device__ __forceinline__ void collide_shifted(typename L::V (&h)[S::Q], const 
         for (int d = 1; d < S::D; ++d) uu = L::fma(u[d], u[d], uu);
         const V c = L::mul(uu, L::set(-1.5f));
         if constexpr (COLL == LGB_BGK) {
-            const V om = L::set((float)cp.omega);
-            {
-                V e0, dummy;
-                shifted_feq_pair<S, L>(0, drho, rho, u, c, e0, dummy);
-                h[0] = L::fma(om, L::sub(e0, h[0]), h[0]);
+            // h' = (1 - w) h + omega heq with omega folded into the
+            // per-weight-class factors omega w rho and omega w drho:
+            //   omega heq_q = omega w rho (b +- 3 e.u) + omega w drho,
+            //   b = 4.5 (e.u)^2 - 1.5 u.u
+            const V om1 = L::set((float)(1.0 - cp.omega));
+            const V omr = L::mul(L::set((float)cp.omega), rho);
+            const V omd = L::mul(L::set((float)cp.omega), drho);
+            V wr[4], wd[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int q = weight_class_rep<S>(k);
+                if (q < 0) continue;
+                wr[k] = L::mul(omr, L::set((float)S::w(q)));
+                wd[k] = L::mul(omd, L::set((float)S::w(q)));
             }
+            h[0] = L::fma(om1, h[0], L::fma(wr[0], c, wd[0]));
 #pragma unroll
             for (int q = 1; q < S::Q; ++q) {
                 const int o = S::opp(q);
                 if (o < q) continue;
-                V eq, eo;
-                shifted_feq_pair<S, L>(q, drho, rho, u, c, eq, eo);
-                h[q] = L::fma(om, L::sub(eq, h[q]), h[q]);
-                h[o] = L::fma(om, L::sub(eo, h[o]), h[o]);
+                const int k = weight_class<S>(q);
+                const V eu = dot_e_u<S, L>(q, u);
+                const V b = L::fma(L::mul(eu, L::set(4.5f)), eu, c);
+                const V p = L::fma(eu, L::set(3.0f), b);
+                const V m = L::fma(eu, L::set(-3.0f), b);
+                h[q] = L::fma(om1, h[q], L::fma(wr[k], p, wd[k]));
+                h[o] = L::fma(om1, h[o], L::fma(wr[k], m, wd[k]));
             }
         } else {  // TRT
             const V ap = L::set((float)cp.inv_2tp), am = L::set((float)cp.inv_2tm);

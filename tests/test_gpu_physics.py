@@ -117,8 +117,8 @@ def test_bounce_back_and_equilibrium_operators(lgb):
     b = lt.EquilibriumBoundaryPU(flow.context, flow, torch.ones(f0.shape[1:], dtype=torch.bool),
                                  [0.1, 0.0, -0.05], 0.01)
     out = to_np(b(flow))
-    rho = flow.units.convert_pressure_pu_to_density_lu(0.01)
-    # a list becomes a float32 tensor in checked_tensor, as in lettuce
+    # numbers and lists become float32 tensors in checked_tensor, as in lettuce
+    rho = flow.units.convert_pressure_pu_to_density_lu(torch.tensor(0.01).to(F64)).item()
     u = torch.as_tensor([0.1, 0.0, -0.05]).to(F64).view(3, 1, 1, 1) \
         * flow.units.characteristic_velocity_lu
     feq = lt.QuadraticEquilibrium()(flow, rho * torch.ones([1] + list(f0.shape[1:]),
