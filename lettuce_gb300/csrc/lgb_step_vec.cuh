@@ -48,8 +48,10 @@ __device__ __forceinline__ uint32_t load_pair(const uint32_t *__restrict__ row, 
     return __byte_perm(__ldg(row + tz), __ldg(row + tzp), 0x5432);
 }
 
+// four resident blocks per SM (64 registers): occupancy hides the load latency
+// better than the registers the compiler would otherwise spend
 template <int SID, int ST, int COLL, int PAT>
-__global__ void __launch_bounds__(256) step_vec2_kernel(const StepParams p) {
+__global__ void __launch_bounds__(256, 4) step_vec2_kernel(const StepParams p) {
     using S = Stencil<SID>;
     using P = Pack16<ST>;
     const uint32_t Zh = p.Z >> 1;
