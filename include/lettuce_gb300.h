@@ -139,6 +139,32 @@ int lgb_reduce(int32_t stencil, int32_t storage, const int32_t *res,
                const int32_t *hi, const uint8_t *mask, double *out,
                void *scratch, void *stream);
 
+/* The same float64 reductions as lgb_reduce, for callers that cannot
+ * allocate device memory: for example a host code whose device memory is
+ * entirely reserved by another allocator (a framework's caching pool, a
+ * fixed arena of a Fortran/C solver), or a latency-critical loop where the
+ * implicit device synchronisation of cudaMalloc is not acceptable. No
+ * counterpart in lettuce (its reductions are torch calls that allocate).
+ *
+ * Scratch: a file-scope device array of LGB_REDUCE_STATIC_SCRATCH_BYTES
+ * (48,640 bytes), held by every GPU that loads this library until the
+ * process exits. The reduction's scratch need does not grow with the field
+ * (a fixed grid of partial sums), so every grid the library accepts fits; a
+ * need above the array size is rejected with an error. The call allocates
+ * nothing (no cudaMalloc, no allocating library routine).
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. All calls share the one array: calls that
+ * overlap on the GPU (different streams, no ordering between them) race and
+ * corrupt each other's results -- order them (same stream or events). The
+ * array keeps the last call's partial sums; each call writes every partial
+ * it reads, so nothing needs clearing. */
+#define LGB_REDUCE_STATIC_SCRATCH_BYTES 48640
+int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res,
+                      const void *f, int32_t aa_pending, const int32_t *lo,
+                      const int32_t *hi, const uint8_t *mask, double *out,
+                      void *stream);
+
 /* Copy a population field between storage formats (for example float32
  * values into LGB_F16_SHIFTED storage and back). Replaces the dtype casts of
  * lettuce/_context.py:97-115 for the population field. */

@@ -26,7 +26,8 @@ FLAG_INDEX_MASK, FLAG_NO_STREAM = 0x1F, 0x80
 OPT_ONE_CELL = 1
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
-            "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_convert"]
+            "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_reduce_static", "lgb_convert"]
+REDUCE_STATIC_SCRATCH_BYTES = 48640
 
 
 class Substep(ctypes.Structure):
@@ -96,6 +97,8 @@ def load():
         L.lgb_reduce_scratch_bytes.restype = I64
         L.lgb_reduce.argtypes = [I32, I32, P, P, I32, P, P, P, P, P, P]
         L.lgb_reduce.restype = ctypes.c_int
+        L.lgb_reduce_static.argtypes = [I32, I32, P, P, I32, P, P, P, P, P]
+        L.lgb_reduce_static.restype = ctypes.c_int
         L.lgb_convert.argtypes = [I32, I32, P, I32, P, I64, P]
         L.lgb_convert.restype = ctypes.c_int
         if L.lgb_abi_version() != ABI_VERSION:

@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "lettuce_gb300.h"
@@ -505,6 +506,79 @@ int lgb_reduce(int32_t stencil, int32_t storage, const int32_t *res, const void 
     cudaError_t e = reduce_dispatch(stencil, storage, g, f, aa_pending, box, mask, out,
                                     static_cast<double *>(scratch), static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "lgb_reduce: launch failed");
+    return 0;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------------------
+// Allocation-free reduction: lgb_reduce with its partial-sum scratch in a
+// file-scope device array instead of a caller-provided buffer. The array is
+// part of this library's device image, so every GPU that loads the library
+// holds it (LGB_REDUCE_STATIC_SCRATCH_BYTES) until the process exits.
+
+static __device__ __align__(256) double g_reduce_scratch[LGB_REDUCE_STATIC_SCRATCH_BYTES / sizeof(double)];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void *g_scratch_addr[kMaxDevices] = {};
+
+// device address of g_reduce_scratch on the current device, looked up once
+// per device (the host-side name g_reduce_scratch is not a device address)
+int static_scratch_address(void **ptr) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "lgb_reduce_static: cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail("lgb_reduce_static: device ordinal %d beyond the %d supported", dev, kMaxDevices);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "lgb_reduce_static: cudaGetSymbolAddress");
+        g_scratch_addr[dev] = p;
+    }
+    *ptr = g_scratch_addr[dev];
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res, const void *f,
+                      int32_t aa_pending, const int32_t *lo, const int32_t *hi,
+                      const uint8_t *mask, double *out, void *stream) {
+    Grid g;
+    if (make_grid(stencil, res, &g)) return -1;
+    if (!valid_storage(storage)) return fail("lgb_reduce_static: unknown storage id %d", storage);
+    if (!f || !out) return fail("lgb_reduce_static: NULL pointer");
+    // the partial sums this reduction writes; it launches a fixed grid of
+    // kReduceBlocks blocks whatever the field size
+    const int64_t need = lgb_reduce_scratch_bytes();
+    if (need > (int64_t)LGB_REDUCE_STATIC_SCRATCH_BYTES)
+        return fail("lgb_reduce_static: the reduction needs %lld bytes of scratch, the static "
+                    "array holds %lld", (long long)need, (long long)LGB_REDUCE_STATIC_SCRATCH_BYTES);
+    ReduceBox box;
+    const uint32_t full[3] = {g.X, g.Y, g.Z};
+    for (int i = 0; i < 3; ++i) { box.lo[i] = 0; box.hi[i] = full[i]; }
+    const int off = 3 - g.d;
+    for (int i = 0; i < g.d; ++i) {
+        const int32_t l = lo ? lo[i] : 0, h = hi ? hi[i] : (int32_t)full[off + i];
+        if (l < 0 || h > (int32_t)full[off + i] || l > h)
+            return fail("lgb_reduce_static: box [%d, %d) invalid along dimension %d", l, h, i);
+        box.lo[off + i] = (uint32_t)l;
+        box.hi[off + i] = (uint32_t)h;
+    }
+    void *scratch = nullptr;
+    if (static_scratch_address(&scratch)) return -1;
+    // every partial row the final fold reads is written earlier in the same
+    // call, so the array needs no clearing between calls
+    cudaError_t e = reduce_dispatch(stencil, storage, g, f, aa_pending, box, mask, out,
+                                    static_cast<double *>(scratch), static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "lgb_reduce_static: launch failed");
     return 0;
 }
 
