@@ -165,6 +165,63 @@ int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res,
                       const int32_t *hi, const uint8_t *mask, double *out,
                       void *stream);
 
+/* ---- batched domains ---------------------------------------------------
+ * Many periodic domains of different sizes, all with the same stencil,
+ * storage and collision kind, advanced by one launch (the batched Taylor-
+ * Green configuration; lettuce advances one Flow per Simulation and has no
+ * counterpart). Domain b's populations are [Q][N_b] at element `offset` of
+ * one pool; its relaxation times are per domain. */
+typedef struct {
+    int64_t offset;     /* element offset of the domain's [Q][N_b] field in the pool */
+    int32_t res[3];     /* lettuce resolution; unused trailing dims = 1 */
+    int32_t reserved;
+    double tau;         /* BGK tau / TRT tau_plus */
+    double tau_minus;   /* TRT */
+} lgb_batch_domain;
+
+typedef struct {
+    int32_t domain;     /* index into the domain table */
+    int32_t row_begin;  /* rows = cells along all but the last lettuce dimension */
+    int32_t row_end;
+    int32_t reserved;
+} lgb_batch_tile;
+
+typedef struct {
+    int32_t abi_version;
+    int32_t stencil;
+    int32_t storage;
+    int32_t collision;   /* LGB_NO_COLLISION, LGB_BGK or LGB_TRT */
+    int32_t n_domains;
+    int32_t n_tiles;
+    int32_t threads;     /* threads per block (multiple of 32, <= 512) */
+    int32_t blocks;      /* resident blocks of the persistent grid */
+    const lgb_batch_domain *domains;  /* device copy of the domain table */
+    const lgb_batch_tile *tiles;      /* device copy of the tile table */
+    const void *f_in;    /* pool read this step */
+    void *f_out;         /* pool written this step (pull pattern) */
+    int64_t pool_elements;
+    uint32_t *status;    /* optional; bit 0 non-finite density, bit 1 a tile
+                            outside its domain or the pool (skipped) */
+} lgb_batch_desc;
+
+/* Host-only: cut every domain into tiles of whole rows holding about
+ * `tile_cells` cells. With tiles == NULL only counts. Returns 0 and the
+ * count in *n_tiles; fails if max_tiles is too small. */
+int lgb_batch_plan(int32_t stencil, int32_t n_domains, const lgb_batch_domain *domains,
+                   int32_t tile_cells, lgb_batch_tile *tiles, int32_t max_tiles,
+                   int32_t *n_tiles);
+/* One pull-pattern step (lettuce PRE_STREAMING) of every domain. */
+int lgb_batched_step(const lgb_batch_desc *desc, void *stream);
+
+/* Adjoint of one pull-pattern BGK step (lettuce PRE_STREAMING order):
+ * lam = (d f_{n+1} / d f_n)^T lam_next, with f_n the state before the step.
+ * float32 or float64 storage; lam must not alias f_n or lam_next. The
+ * reverse pass of a differentiable rollout (torch autograd through
+ * lettuce's step, lettuce/_simulation.py:241-305, computes the same
+ * product); lettuce has no hand-written adjoint. */
+int lgb_adjoint_step(int32_t stencil, int32_t storage, const int32_t *res, double tau,
+                     const void *f_n, const void *lam_next, void *lam, void *stream);
+
 /* Copy a population field between storage formats (for example float32
  * values into LGB_F16_SHIFTED storage and back). Replaces the dtype casts of
  * lettuce/_context.py:97-115 for the population field. */

@@ -21,6 +21,8 @@ from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporte
                         MaximumVelocity, NaNReporter, Observable, ObservableReporter)
 from ._flows import ExtFlow, Obstacle, TaylorGreenVortex
 from ._native import NativeBoundary, NativeCollision, NativeEquilibrium
+from ._batched import BatchedSimulation, batched_taylor_green
+from ._adjoint import moments_torch, rollout
 
 __version__ = "0.1.0"
 
@@ -34,5 +36,6 @@ __all__ = [
     "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",
     "Enstrophy", "EnergySpectrum", "Mass", "ErrorReporter", "FailureReporterBase",
     "NaNReporter", "HighMaReporter", "ExtFlow", "TaylorGreenVortex", "Obstacle",
-    "NativeBoundary", "NativeCollision", "NativeEquilibrium",
+    "NativeBoundary", "NativeCollision", "NativeEquilibrium", "BatchedSimulation",
+    "batched_taylor_green", "rollout", "moments_torch",
 ]

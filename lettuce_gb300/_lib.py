@@ -26,7 +26,8 @@ FLAG_INDEX_MASK, FLAG_NO_STREAM = 0x1F, 0x80
 OPT_ONE_CELL = 1
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
-            "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_reduce_static", "lgb_convert"]
+            "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_reduce_static", "lgb_convert",
+            "lgb_batch_plan", "lgb_batched_step", "lgb_adjoint_step"]
 REDUCE_STATIC_SCRATCH_BYTES = 48640
 
 
@@ -100,6 +101,8 @@ def load():
         L.lgb_reduce_static.argtypes = [I32, I32, P, P, I32, P, P, P, P, P]
         L.lgb_reduce_static.restype = ctypes.c_int
         L.lgb_convert.argtypes = [I32, I32, P, I32, P, I64, P]
+        L.lgb_adjoint_step.argtypes = [I32, I32, P, ctypes.c_double, P, P, P, P]
+        L.lgb_adjoint_step.restype = ctypes.c_int
         L.lgb_convert.restype = ctypes.c_int
         if L.lgb_abi_version() != ABI_VERSION:
             raise LibraryError(f"{path} has ABI version {L.lgb_abi_version()}, "

@@ -30,6 +30,17 @@ int fail(const char *fmt, ...) {
     return -1;
 }
 
+}  // namespace
+
+namespace lgb {
+int set_error(const char *msg) {
+    g_last_error = msg;
+    return -1;
+}
+}  // namespace lgb
+
+namespace {
+
 int cuda_fail(cudaError_t e, const char *what) {
     return fail("%s: %s", what, cudaGetErrorString(e));
 }

@@ -1,0 +1,126 @@
+// Batched step: many periodic domains of uneven sizes advanced by one
+// persistent launch. All domains' population fields live in one pool (domain
+// b at element offset `offset`, layout [Q][N_b] as for a single grid); the
+// host cuts every domain into tiles of whole rows (lgb_batch_plan) and the
+// kernel's resident blocks walk the tile table with a grid stride, one cell
+// per thread, pulling from the periodic neighbours inside the tile's domain.
+// The per-domain relaxation times come from the domain table.
+#pragma once
+
+#include "lgb_shifted.cuh"
+#include "lgb_step.cuh"
+
+namespace lgb {
+
+struct BatchParams {
+    const void *f_in;
+    void *f_out;
+    const lgb_batch_domain *domains;
+    const lgb_batch_tile *tiles;
+    int32_t n_domains;
+    int32_t n_tiles;
+    int64_t pool_elements;
+    uint32_t *status;
+};
+
+template <int SID, int ST, int COLL>
+__global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) {
+    using S = Stencil<SID>;
+    using Sto = Storage<ST>;
+    using R = typename Sto::R;
+    using T = typename Sto::T;
+    constexpr bool HSPACE = is_shifted<ST>() && shifted_collision<COLL>();
+    const T *__restrict__ pool_in = static_cast<const T *>(p.f_in);
+    T *pool_out = static_cast<T *>(p.f_out);
+    for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
+        const lgb_batch_tile tile = p.tiles[t];
+        if (tile.domain < 0 || tile.domain >= p.n_domains) {
+            if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
+            continue;
+        }
+        const lgb_batch_domain dom = p.domains[tile.domain];
+        // the domain as an internal (X, Y, Z) grid
+        StepParams g;
+        const int d = S::D;
+        uint32_t r[3] = {1, 1, 1};
+        bool ok = true;
+        for (int i = 0; i < d; ++i) {
+            ok = ok && dom.res[i] > 0;
+            r[3 - d + i] = (uint32_t)dom.res[i];
+        }
+        g.X = r[0]; g.Y = r[1]; g.Z = r[2];
+        const uint64_t n64 = (uint64_t)r[0] * r[1] * r[2];
+        // the tile must lie inside its domain and the domain inside the pool
+        ok = ok && n64 < (1ull << 32) && dom.offset >= 0 &&
+             (uint64_t)dom.offset + (uint64_t)S::Q * n64 <= (uint64_t)p.pool_elements &&
+             tile.row_begin >= 0 && tile.row_begin <= tile.row_end &&
+             (uint64_t)tile.row_end <= (uint64_t)r[0] * r[1] && dom.tau > 0.0;
+        if (!ok) {
+            if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
+            continue;
+        }
+        g.N = (uint32_t)n64;
+        const FastDiv divZ = FastDiv::make_device(g.Z), divY = FastDiv::make_device(g.Y);
+        CollideParams cp;
+        cp.omega = 1.0 / dom.tau;
+        cp.inv_2tp = 1.0 / (2.0 * dom.tau);
+        cp.inv_2tm = 1.0 / (2.0 * dom.tau_minus);
+        cp.beta = 1.0 / (2.0 * dom.tau);
+        const T *__restrict__ fin = pool_in + dom.offset;
+        T *fout = pool_out + dom.offset;
+        const uint32_t first = (uint32_t)tile.row_begin * g.Z;
+        const uint32_t last = (uint32_t)tile.row_end * g.Z;
+        for (uint32_t n = first + threadIdx.x; n < last; n += blockDim.x) {
+            const uint32_t row = divZ.div(n);
+            const uint32_t z = n - row * g.Z;
+            const uint32_t x = divY.div(row);
+            const uint32_t y = row - x * g.Y;
+            Nbr c;
+            c.set(x, y, z, g);
+            R f[S::Q];
+            load_cell<S, Sto, LOAD_PULL, false, HSPACE>(g, fin, c, n, 0u, f);
+            if constexpr (HSPACE) {
+                collide_shifted<S, Lane1, COLL>(f, cp);
+            } else {
+                R rr;
+                collide<COLL, S>(f, cp, rr);
+            }
+            if (p.status) {
+                R s = R(0);
+#pragma unroll
+                for (int q = 0; q < S::Q; ++q) s += f[q];
+                if (!isfinite(s)) atomicOr(p.status, 1u);
+            }
+            const size_t N = g.N;
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) store_value<Sto, HSPACE>(fout + (size_t)q * N + n, f[q], S::w(q));
+        }
+    }
+}
+
+template <int SID, int ST>
+cudaError_t launch_batched(int coll, const BatchParams &p, int blocks, int threads, cudaStream_t s) {
+    switch (coll) {
+    case LGB_NO_COLLISION:
+        batched_step_kernel<SID, ST, LGB_NO_COLLISION><<<blocks, threads, 0, s>>>(p);
+        break;
+    case LGB_BGK: batched_step_kernel<SID, ST, LGB_BGK><<<blocks, threads, 0, s>>>(p); break;
+    case LGB_TRT: batched_step_kernel<SID, ST, LGB_TRT><<<blocks, threads, 0, s>>>(p); break;
+    default: return cudaErrorNotSupported;
+    }
+    return cudaGetLastError();
+}
+
+template <int SID>
+cudaError_t dispatch_batched(int storage, int coll, const BatchParams &p, int blocks, int threads,
+                             cudaStream_t s) {
+    switch (storage) {
+    case LGB_F64: return launch_batched<SID, LGB_F64>(coll, p, blocks, threads, s);
+    case LGB_F32: return launch_batched<SID, LGB_F32>(coll, p, blocks, threads, s);
+    case LGB_F16_SHIFTED: return launch_batched<SID, LGB_F16_SHIFTED>(coll, p, blocks, threads, s);
+    case LGB_BF16_SHIFTED: return launch_batched<SID, LGB_BF16_SHIFTED>(coll, p, blocks, threads, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace lgb

@@ -34,6 +34,15 @@ struct FastDiv {
         f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
         return f;
     }
+    // the same magic numbers computed on the device (per tile of a batch)
+    __device__ __forceinline__ static FastDiv make_device(uint32_t d) {
+        FastDiv f;
+        f.d = d;
+        const uint32_t l = d <= 1 ? 0u : 32u - __clz(d - 1);
+        f.s = l;
+        f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+        return f;
+    }
     __device__ __forceinline__ uint32_t div(uint32_t n) const {
         if (s == 0) return n;
         const uint32_t t = __umulhi(m, n);
