@@ -228,26 +228,50 @@ __device__ __forceinline__ void store_value(typename Sto::T *ptr, typename Sto::
     else Sto::store(ptr, v, w);
 }
 
-template <int SID, int ST, int COLL, int PAT, bool MASKED>
+// MASK: 0 = no boundaries; 1 = boundaries, every cell except those of the
+// anti-bounce-back outlet plane (when there is one); 2 = the outlet plane
+// only (one thread per plane cell). Splitting the outlet off keeps its extra
+// neighbour reconstruction out of the register budget of the bulk launch.
+template <int SID, int ST, int COLL, int PAT, int MASK>
 __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     using S = Stencil<SID>;
     using Sto = Storage<ST>;
     using R = typename Sto::R;
     using T = typename Sto::T;
+    constexpr bool MASKED = MASK != 0;
+    constexpr bool SUBSTEPS = PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK;
     constexpr int LOAD = PatternTraits<PAT>::load;
     // 16-bit formats without boundaries collide in shifted space, with the
     // same arithmetic as the two-cell kernel
     constexpr bool HSPACE = is_shifted<ST>() && !MASKED && shifted_collision<COLL>();
     const T *__restrict__ fin = static_cast<const T *>(p.f_in);
     T *fout = static_cast<T *>(p.f_out);
-    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.N) return;
-    const uint32_t row = p.divZ.div(n);
-    const uint32_t z = n - row * p.Z;
-    const uint32_t x = p.divY.div(row);
-    const uint32_t y = row - x * p.Y;
+    uint32_t n, x, y, z;
+    if constexpr (MASK == 2) {
+        // plane cell i -> (x, y, z) with the normal coordinate fixed
+        const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+        const uint32_t a = p.abb_axis == 0 ? p.Y : p.X;  // first free axis extent
+        const uint32_t b = p.abb_axis == 2 ? p.Y : p.Z;  // second (fastest) free axis
+        if (i >= a * b) return;
+        const uint32_t u0 = i / b, u1 = i - u0 * b;
+        if (p.abb_axis == 0) { x = p.abb_plane; y = u0; z = u1; }
+        else if (p.abb_axis == 1) { x = u0; y = p.abb_plane; z = u1; }
+        else { x = u0; y = u1; z = p.abb_plane; }
+        n = (x * p.Y + y) * p.Z + z;
+    } else {
+        n = blockIdx.x * blockDim.x + threadIdx.x;
+        if (n >= p.N) return;
+        const uint32_t row = p.divZ.div(n);
+        z = n - row * p.Z;
+        x = p.divY.div(row);
+        y = row - x * p.Y;
+    }
     Nbr c;
     c.set(x, y, z, p);
+    if constexpr (MASK == 1 && SUBSTEPS) {
+        // the outlet plane has its own launch
+        if (p.abb_k >= 0 && coord_along(c, p.abb_axis) == p.abb_plane) return;
+    }
 
     uint8_t fl = 0;
     uint32_t nsbits = 0;
@@ -262,9 +286,12 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
         if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK)
             collide_shifted<S, Lane1, COLL>(f, p.cp);
     } else if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
-        if constexpr (MASKED) {
-            // a cell runs the substep its index names, and the outlet
-            // substep if it lies on the outlet plane, in sequence order
+        if constexpr (MASK == 1) {
+            // a cell off the outlet plane runs the substep its index names
+            apply_local_substep<S, COLL>(p, select_sub(p, fl & LGB_FLAG_INDEX_MASK), c, f);
+        } else if constexpr (MASK == 2) {
+            // an outlet-plane cell runs the substep its index names and the
+            // outlet substep, in sequence order
             const int idx = fl & LGB_FLAG_INDEX_MASK;
             const bool outlet = p.abb_k >= 0 && coord_along(c, p.abb_axis) == p.abb_plane;
             const int outlet_phase = p.abb_k < idx ? 0 : 1;
@@ -312,28 +339,51 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     }
 }
 
-template <int SID, int ST, int COLL, int PAT, bool MASKED>
+template <int SID, int ST, int COLL, int PAT, int MASK>
 cudaError_t launch_step(const StepParams &p, cudaStream_t stream) {
     const unsigned threads = 256;
-    const unsigned blocks = (unsigned)((p.N + threads - 1) / threads);
-    step_kernel<SID, ST, COLL, PAT, MASKED><<<blocks, threads, 0, stream>>>(p);
+    uint64_t count = p.N;
+    if (MASK == 2) {
+        const uint32_t ax = p.abb_axis == 0 ? p.X : (p.abb_axis == 1 ? p.Y : p.Z);
+        count = p.N / ax;
+    }
+    const unsigned blocks = (unsigned)((count + threads - 1) / threads);
+    step_kernel<SID, ST, COLL, PAT, MASK><<<blocks, threads, 0, stream>>>(p);
     return cudaGetLastError();
 }
 
 // collision kinds that are instantiated for a stencil
 template <int SID> constexpr bool has_kbc() { return SID == LGB_D2Q9 || SID == LGB_D3Q27; }
 
+// with boundaries: the bulk launch (MASK 1) and, if there is an outlet and
+// the pattern has substeps, the outlet-plane launch (MASK 2)
+template <int SID, int ST, int COLL, int PAT, bool MASKED>
+cudaError_t launch_step_set(const StepParams &p, cudaStream_t s) {
+    if constexpr (!MASKED) {
+        return launch_step<SID, ST, COLL, PAT, 0>(p, s);
+    } else {
+        cudaError_t e = launch_step<SID, ST, COLL, PAT, 1>(p, s);
+        if (e != cudaSuccess) return e;
+        constexpr bool SUBSTEPS = PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK;
+        constexpr bool OUTLET = SUBSTEPS && PAT != LGB_AA_EVEN && PAT != LGB_AA_ODD;
+        if constexpr (OUTLET) {
+            if (p.abb_k >= 0) return launch_step<SID, ST, COLL, PAT, 2>(p, s);
+        }
+        return cudaSuccess;
+    }
+}
+
 template <int SID, int ST, int PAT, bool MASKED>
 cudaError_t dispatch_collision(int coll, const StepParams &p, cudaStream_t s) {
     if constexpr (PAT == LGB_STREAM_ONLY || PAT == LGB_AA_UNPACK) {
-        return launch_step<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+        return launch_step_set<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
     } else {
     switch (coll) {
-    case LGB_NO_COLLISION: return launch_step<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
-    case LGB_BGK: return launch_step<SID, ST, LGB_BGK, PAT, MASKED>(p, s);
-    case LGB_TRT: return launch_step<SID, ST, LGB_TRT, PAT, MASKED>(p, s);
+    case LGB_NO_COLLISION: return launch_step_set<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+    case LGB_BGK: return launch_step_set<SID, ST, LGB_BGK, PAT, MASKED>(p, s);
+    case LGB_TRT: return launch_step_set<SID, ST, LGB_TRT, PAT, MASKED>(p, s);
     case LGB_KBC:
-        if constexpr (has_kbc<SID>()) return launch_step<SID, ST, LGB_KBC, PAT, MASKED>(p, s);
+        if constexpr (has_kbc<SID>()) return launch_step_set<SID, ST, LGB_KBC, PAT, MASKED>(p, s);
         return cudaErrorNotSupported;
     }
     return cudaErrorInvalidValue;
