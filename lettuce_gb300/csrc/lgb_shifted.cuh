@@ -8,8 +8,12 @@
 //
 // The arithmetic is written once over a lane type L: L = Lane1 (one cell per
 // thread, float) or Lane2 (two cells per thread, float2 with the packed
-// f32x2 instructions of sm_100+). Every operation is an explicit
-// round-to-nearest intrinsic, so both give bit-identical per-cell results.
+// f32x2 instructions of sm_100+). Both give bit-identical per-cell results
+// because every operation is an explicit round-to-nearest intrinsic AND no
+// product is ever an operand of an add or subtract: the compiler fuses a
+// packed multiply into a following packed add (the scalar __fmul_rn is never
+// fused), so every multiply-add here is written as an explicit FMA and e.u
+// and u.u are formed from sums of j before the single scaling by 1/rho.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -40,75 +44,59 @@ struct Lane2 {
     static __device__ __forceinline__ V rcp(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 };
 
-// density deviation, density and velocity of shifted populations
+// density deviation, density, 1/density and momentum of shifted populations
 template <class S, class L>
 __device__ __forceinline__ void shifted_moments(const typename L::V (&h)[S::Q], typename L::V &drho,
-                                                typename L::V &rho, typename L::V (&u)[3]) {
+                                                typename L::V &rho, typename L::V &inv,
+                                                typename L::V (&j)[3]) {
     using V = typename L::V;
     V r = h[0];
 #pragma unroll
     for (int q = 1; q < S::Q; ++q) r = L::add(r, h[q]);
     drho = r;
     rho = L::add(r, L::set(1.0f));
-    const V inv = L::rcp(rho);
+    inv = L::rcp(rho);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) u[d] = L::set(0.0f);
+    for (int d = 0; d < 3; ++d) j[d] = L::set(0.0f);
 #pragma unroll
     for (int d = 0; d < S::D; ++d) {
-        V j = L::set(0.0f);
+        V acc = L::set(0.0f);
         bool first = true;
 #pragma unroll
         for (int q = 1; q < S::Q; ++q) {
             const int c = S::e(q, d);
             if (c == 0) continue;
-            if (first) { j = c > 0 ? h[q] : L::sub(L::set(0.0f), h[q]); first = false; }
-            else j = c > 0 ? L::add(j, h[q]) : L::sub(j, h[q]);
+            if (first) { acc = c > 0 ? h[q] : L::sub(L::set(0.0f), h[q]); first = false; }
+            else acc = c > 0 ? L::add(acc, h[q]) : L::sub(acc, h[q]);
         }
-        u[d] = L::mul(j, inv);
+        j[d] = acc;
     }
 }
 
-// e_q . u for a compile-time q
+// e_q . x for a compile-time q (sums and differences only)
 template <class S, class L>
-__device__ __forceinline__ typename L::V dot_e_u(int q, const typename L::V (&u)[3]) {
+__device__ __forceinline__ typename L::V dot_e(int q, const typename L::V (&x)[3]) {
     using V = typename L::V;
-    V eu = L::set(0.0f);
+    V r = L::set(0.0f);
     bool first = true;
 #pragma unroll
     for (int d = 0; d < S::D; ++d) {
         const int c = S::e(q, d);
         if (c == 0) continue;
-        if (first) { eu = c > 0 ? u[d] : L::sub(L::set(0.0f), u[d]); first = false; }
-        else eu = c > 0 ? L::add(eu, u[d]) : L::sub(eu, u[d]);
+        if (first) { r = c > 0 ? x[d] : L::sub(L::set(0.0f), x[d]); first = false; }
+        else r = c > 0 ? L::add(r, x[d]) : L::sub(r, x[d]);
     }
-    return eu;
+    return r;
 }
 
-// weight class of a velocity: |e|^2 (0 rest, 1 axis, 2 face diagonal,
-// 3 space diagonal); every lettuce stencil has one weight per class
-template <class S> __host__ __device__ constexpr int weight_class(int q) {
-    int s = 0;
-    for (int d = 0; d < S::D; ++d) s += S::e(q, d) * S::e(q, d);
-    return s;
-}
-// first velocity of class k, or -1 when the stencil has none
-template <class S> __host__ __device__ constexpr int weight_class_rep(int k) {
-    for (int q = 0; q < S::Q; ++q)
-        if (weight_class<S>(q) == k) return q;
-    return -1;
-}
-
-// shifted equilibria of the pair (q, opposite(q)): they share e.u up to sign
+// b +- 3 e.u for the pair (q, opposite(q)), b = 4.5 (e.u)^2 - 1.5 u.u;
+// c = -1.5 u.u, eu = (e_q . j) / rho
 template <class S, class L>
-__device__ __forceinline__ void shifted_feq_pair(int q, typename L::V drho, typename L::V rho,
-                                                 const typename L::V (&u)[3], typename L::V c,
-                                                 typename L::V &heq_q, typename L::V &heq_o) {
-    using V = typename L::V;
-    const V a = L::mul(dot_e_u<S, L>(q, u), L::set(3.0f));
-    const V b = L::fma(L::mul(a, L::set(0.5f)), a, c);  // c = -1.5 u.u
-    const V wq = L::set((float)S::w(q));
-    heq_q = L::mul(wq, L::fma(rho, L::add(b, a), drho));
-    heq_o = L::mul(wq, L::fma(rho, L::sub(b, a), drho));
+__device__ __forceinline__ void pair_terms(typename L::V eu, typename L::V c, typename L::V &p,
+                                           typename L::V &m) {
+    const typename L::V b = L::fma(L::mul(eu, L::set(4.5f)), eu, c);
+    p = L::fma(eu, L::set(3.0f), b);
+    m = L::fma(eu, L::set(-3.0f), b);
 }
 
 template <class S, class L, int COLL>
@@ -117,60 +105,54 @@ __device__ __forceinline__ void collide_shifted(typename L::V (&h)[S::Q], const 
     if constexpr (COLL == LGB_NO_COLLISION) {
         return;
     } else {
-        V drho, rho, u[3];
-        shifted_moments<S, L>(h, drho, rho, u);
-        V uu = L::mul(u[0], u[0]);
+        V drho, rho, inv, j[3];
+        shifted_moments<S, L>(h, drho, rho, inv, j);
+        // u.u = (j.j) / rho^2, c = -1.5 u.u
+        V jj = L::mul(j[0], j[0]);
 #pragma unroll
-        for (int d = 1; d < S::D; ++d) uu = L::fma(u[d], u[d], uu);
-        const V c = L::mul(uu, L::set(-1.5f));
+        for (int d = 1; d < S::D; ++d) jj = L::fma(j[d], j[d], jj);
+        const V c = L::mul(L::mul(jj, L::mul(inv, inv)), L::set(-1.5f));
         if constexpr (COLL == LGB_BGK) {
-            // h' = (1 - w) h + omega heq with omega folded into the
-            // per-weight-class factors omega w rho and omega w drho:
-            //   omega heq_q = omega w rho (b +- 3 e.u) + omega w drho,
-            //   b = 4.5 (e.u)^2 - 1.5 u.u
+            // h' = (1 - omega) h + omega heq, omega folded into the factors
+            // omega w rho and omega w drho: omega heq_q = fma(omega w rho, b +- 3 e.u, omega w drho)
             const V om1 = L::set((float)(1.0 - cp.omega));
             const V omr = L::mul(L::set((float)cp.omega), rho);
             const V omd = L::mul(L::set((float)cp.omega), drho);
-            V wr[4], wd[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int q = weight_class_rep<S>(k);
-                if (q < 0) continue;
-                wr[k] = L::mul(omr, L::set((float)S::w(q)));
-                wd[k] = L::mul(omd, L::set((float)S::w(q)));
-            }
-            h[0] = L::fma(om1, h[0], L::fma(wr[0], c, wd[0]));
+            h[0] = L::fma(om1, h[0], L::fma(L::mul(omr, L::set((float)S::w(0))), c,
+                                            L::mul(omd, L::set((float)S::w(0)))));
 #pragma unroll
             for (int q = 1; q < S::Q; ++q) {
                 const int o = S::opp(q);
                 if (o < q) continue;
-                const int k = weight_class<S>(q);
-                const V eu = dot_e_u<S, L>(q, u);
-                const V b = L::fma(L::mul(eu, L::set(4.5f)), eu, c);
-                const V p = L::fma(eu, L::set(3.0f), b);
-                const V m = L::fma(eu, L::set(-3.0f), b);
-                h[q] = L::fma(om1, h[q], L::fma(wr[k], p, wd[k]));
-                h[o] = L::fma(om1, h[o], L::fma(wr[k], m, wd[k]));
+                const V wr = L::mul(omr, L::set((float)S::w(q)));
+                const V wd = L::mul(omd, L::set((float)S::w(q)));
+                V p, m;
+                pair_terms<S, L>(L::mul(dot_e<S, L>(q, j), inv), c, p, m);
+                h[q] = L::fma(om1, h[q], L::fma(wr, p, wd));
+                h[o] = L::fma(om1, h[o], L::fma(wr, m, wd));
             }
-        } else {  // TRT
-            const V ap = L::set((float)cp.inv_2tp), am = L::set((float)cp.inv_2tm);
+        } else {  // TRT: h' = h - ap ((h+ho) - (eq+eo)) -/+ am ((h-ho) - (eq-eo))
+            const V nap = L::set((float)-cp.inv_2tp);
+            const V am = L::set((float)cp.inv_2tm), nam = L::set((float)-cp.inv_2tm);
             {
-                V e0, dummy;
-                shifted_feq_pair<S, L>(0, drho, rho, u, c, e0, dummy);
+                const V e0 = L::fma(L::mul(rho, L::set((float)S::w(0))), c,
+                                    L::mul(drho, L::set((float)S::w(0))));
                 const V dp = L::sub(L::add(h[0], h[0]), L::add(e0, e0));
-                h[0] = L::sub(h[0], L::mul(dp, ap));
+                h[0] = L::fma(nap, dp, h[0]);
             }
 #pragma unroll
             for (int q = 1; q < S::Q; ++q) {
                 const int o = S::opp(q);
                 if (o < q) continue;
-                V eq, eo;
-                shifted_feq_pair<S, L>(q, drho, rho, u, c, eq, eo);
+                const V wr = L::mul(rho, L::set((float)S::w(q)));
+                const V wd = L::mul(drho, L::set((float)S::w(q)));
+                V p, m;
+                pair_terms<S, L>(L::mul(dot_e<S, L>(q, j), inv), c, p, m);
+                const V eq = L::fma(wr, p, wd), eo = L::fma(wr, m, wd);
                 const V dp = L::sub(L::add(h[q], h[o]), L::add(eq, eo));
                 const V dm = L::sub(L::sub(h[q], h[o]), L::sub(eq, eo));
-                const V sp = L::mul(dp, ap), sm = L::mul(dm, am);
-                h[q] = L::sub(L::sub(h[q], sp), sm);
-                h[o] = L::add(L::sub(h[o], sp), sm);
+                h[q] = L::fma(nap, dp, L::fma(nam, dm, h[q]));
+                h[o] = L::fma(nap, dp, L::fma(am, dm, h[o]));
             }
         }
     }
