@@ -12,8 +12,9 @@
 // because every operation is an explicit round-to-nearest intrinsic AND no
 // product is ever an operand of an add or subtract: the compiler fuses a
 // packed multiply into a following packed add (the scalar __fmul_rn is never
-// fused), so every multiply-add here is written as an explicit FMA and e.u
-// and u.u are formed from sums of j before the single scaling by 1/rho.
+// fused), so every multiply-add here is written as an explicit FMA, and the
+// equilibrium is expressed through e.j and j.j so that no rounded product of
+// 1/rho feeds a sum.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -89,68 +90,58 @@ __device__ __forceinline__ typename L::V dot_e(int q, const typename L::V (&x)[3
     return r;
 }
 
-// b +- 3 e.u for the pair (q, opposite(q)), b = 4.5 (e.u)^2 - 1.5 u.u;
-// c = -1.5 u.u, eu = (e_q . j) / rho
-template <class S, class L>
-__device__ __forceinline__ void pair_terms(typename L::V eu, typename L::V c, typename L::V &p,
-                                           typename L::V &m) {
-    const typename L::V b = L::fma(L::mul(eu, L::set(4.5f)), eu, c);
-    p = L::fma(eu, L::set(3.0f), b);
-    m = L::fma(eu, L::set(-3.0f), b);
-}
-
 template <class S, class L, int COLL>
 __device__ __forceinline__ void collide_shifted(typename L::V (&h)[S::Q], const CollideParams &cp) {
     using V = typename L::V;
     if constexpr (COLL == LGB_NO_COLLISION) {
         return;
     } else {
+        // With ej = e_q . j and e.u = ej / rho the shifted equilibrium is
+        //   heq_q = w_q X_q,  X_q = base + 3 ej + 4.5 ej^2 / rho,
+        //   base = drho - 1.5 (j.j) / rho,
+        // and the opposite direction has X_o = base - 3 ej + 4.5 ej^2 / rho.
         V drho, rho, inv, j[3];
         shifted_moments<S, L>(h, drho, rho, inv, j);
-        // u.u = (j.j) / rho^2, c = -1.5 u.u
         V jj = L::mul(j[0], j[0]);
 #pragma unroll
         for (int d = 1; d < S::D; ++d) jj = L::fma(j[d], j[d], jj);
-        const V c = L::mul(L::mul(jj, L::mul(inv, inv)), L::set(-1.5f));
+        const V base = L::fma(jj, L::mul(inv, L::set(-1.5f)), drho);
+        const V k45 = L::mul(inv, L::set(4.5f));
         if constexpr (COLL == LGB_BGK) {
-            // h' = (1 - omega) h + omega heq, omega folded into the factors
-            // omega w rho and omega w drho: omega heq_q = fma(omega w rho, b +- 3 e.u, omega w drho)
+            // h' = (1 - omega) h + (omega w_q) X_q
+            const float om = (float)cp.omega;
             const V om1 = L::set((float)(1.0 - cp.omega));
-            const V omr = L::mul(L::set((float)cp.omega), rho);
-            const V omd = L::mul(L::set((float)cp.omega), drho);
-            h[0] = L::fma(om1, h[0], L::fma(L::mul(omr, L::set((float)S::w(0))), c,
-                                            L::mul(omd, L::set((float)S::w(0)))));
+            h[0] = L::fma(L::set(om * (float)S::w(0)), base, L::mul(om1, h[0]));
 #pragma unroll
             for (int q = 1; q < S::Q; ++q) {
                 const int o = S::opp(q);
                 if (o < q) continue;
-                const V wr = L::mul(omr, L::set((float)S::w(q)));
-                const V wd = L::mul(omd, L::set((float)S::w(q)));
-                V p, m;
-                pair_terms<S, L>(L::mul(dot_e<S, L>(q, j), inv), c, p, m);
-                h[q] = L::fma(om1, h[q], L::fma(wr, p, wd));
-                h[o] = L::fma(om1, h[o], L::fma(wr, m, wd));
+                const V ow = L::set(om * (float)S::w(q));
+                const V ej = dot_e<S, L>(q, j);
+                const V sq = L::fma(L::mul(ej, k45), ej, base);
+                h[q] = L::fma(ow, L::fma(ej, L::set(3.0f), sq), L::mul(om1, h[q]));
+                h[o] = L::fma(ow, L::fma(ej, L::set(-3.0f), sq), L::mul(om1, h[o]));
             }
-        } else {  // TRT: h' = h - ap ((h+ho) - (eq+eo)) -/+ am ((h-ho) - (eq-eo))
+        } else {
+            // TRT: with heq_q + heq_o = 2 w s and heq_q - heq_o = 6 w ej,
+            //   dp = (h_q + h_o) - 2 w s,  dm = (h_q - h_o) - 6 w ej,
+            //   h_q' = h_q - dp / (2 tau+) - dm / (2 tau-),
+            //   h_o' = h_o - dp / (2 tau+) + dm / (2 tau-)
             const V nap = L::set((float)-cp.inv_2tp);
             const V am = L::set((float)cp.inv_2tm), nam = L::set((float)-cp.inv_2tm);
             {
-                const V e0 = L::fma(L::mul(rho, L::set((float)S::w(0))), c,
-                                    L::mul(drho, L::set((float)S::w(0))));
-                const V dp = L::sub(L::add(h[0], h[0]), L::add(e0, e0));
+                const V dp = L::fma(L::set(-2.0f * (float)S::w(0)), base, L::add(h[0], h[0]));
                 h[0] = L::fma(nap, dp, h[0]);
             }
 #pragma unroll
             for (int q = 1; q < S::Q; ++q) {
                 const int o = S::opp(q);
                 if (o < q) continue;
-                const V wr = L::mul(rho, L::set((float)S::w(q)));
-                const V wd = L::mul(drho, L::set((float)S::w(q)));
-                V p, m;
-                pair_terms<S, L>(L::mul(dot_e<S, L>(q, j), inv), c, p, m);
-                const V eq = L::fma(wr, p, wd), eo = L::fma(wr, m, wd);
-                const V dp = L::sub(L::add(h[q], h[o]), L::add(eq, eo));
-                const V dm = L::sub(L::sub(h[q], h[o]), L::sub(eq, eo));
+                const float w = (float)S::w(q);
+                const V ej = dot_e<S, L>(q, j);
+                const V sq = L::fma(L::mul(ej, k45), ej, base);
+                const V dp = L::fma(L::set(-2.0f * w), sq, L::add(h[q], h[o]));
+                const V dm = L::fma(L::set(-6.0f * w), ej, L::sub(h[q], h[o]));
                 h[q] = L::fma(nap, dp, L::fma(nam, dm, h[q]));
                 h[o] = L::fma(nap, dp, L::fma(am, dm, h[o]));
             }
