@@ -41,8 +41,12 @@ enum {
     LGB_SUB_BOUNCE_BACK = 1,       /* lettuce/ext/_boundary/bounce_back_boundary.py */
     LGB_SUB_EQUILIBRIUM_PU = 2,    /* lettuce/ext/_boundary/equilibrium_boundary_pu.py */
     LGB_SUB_ANTI_BOUNCE_BACK = 3,  /* lettuce/ext/_boundary/anti_bounce_back_outlet.py */
-    LGB_SUB_NONE = 4
+    LGB_SUB_NONE = 4,
+    LGB_SUB_EQUILIBRIUM_OUTLET_P = 5, /* lettuce/ext/_boundary/equilibrium_outlet_p.py */
+    LGB_SUB_PARTIALLY_SATURATED = 6   /* lettuce/ext/_boundary/partially_saturated_boundary.py */
 };
+/* At most one outlet-plane substep (anti-bounce-back or pressure outlet)
+ * per step descriptor. */
 
 /* memory access pattern of one launch. PULL is stream-then-collide
  * (lettuce PRE_STREAMING), PUSH collide-then-stream (POST_STREAMING), LOCAL
@@ -75,6 +79,9 @@ typedef struct {
     const void *u;
     int64_t rho_stride[3];
     int64_t u_stride[4]; /* component, then lettuce dimensions */
+    /* pressure outlet: param[0] = outlet density (lattice units);
+     * partially saturated: param[0] = tau, param[1] = B(saturation, tau) */
+    double param[2];
 } lgb_substep;
 
 typedef struct {

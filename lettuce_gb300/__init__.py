@@ -14,7 +14,8 @@ from ._unit import UnitConversion
 from ._flow import (Boundary, Equilibrium, Flow, QuadraticEquilibrium,
                     initialize_f_neq, torch_gradient)
 from ._collision import BGKCollision, Collision, KBCCollision, NoCollision, TRTCollision
-from ._boundary import AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU
+from ._boundary import (AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU,
+                        EquilibriumOutletP, PartiallySaturatedBC)
 from ._simulation import BreakableSimulation, Reporter, Simulation, StreamingStrategy
 from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporterBase,
                         HighMaReporter, IncompressibleKineticEnergy, Mass,
@@ -31,7 +32,8 @@ __all__ = [
     "UnitConversion", "Flow", "Equilibrium", "QuadraticEquilibrium", "Boundary",
     "initialize_f_neq", "torch_gradient", "Collision", "BGKCollision",
     "TRTCollision", "KBCCollision", "NoCollision", "BounceBackBoundary",
-    "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "Simulation",
+    "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "EquilibriumOutletP",
+    "PartiallySaturatedBC", "Simulation",
     "BreakableSimulation", "StreamingStrategy", "Reporter", "Observable",
     "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",
     "Enstrophy", "EnergySpectrum", "Mass", "ErrorReporter", "FailureReporterBase",

@@ -3,6 +3,8 @@
 * BounceBackBoundary  -- lettuce/ext/_boundary/bounce_back_boundary.py:10-32
 * EquilibriumBoundaryPU -- lettuce/ext/_boundary/equilibrium_boundary_pu.py:15-98
 * AntiBounceBackOutlet -- lettuce/ext/_boundary/anti_bounce_back_outlet.py:13-109
+* EquilibriumOutletP -- lettuce/ext/_boundary/equilibrium_outlet_p.py:12-91
+* PartiallySaturatedBC -- lettuce/ext/_boundary/partially_saturated_boundary.py:6-51
 
 The masks are built exactly as lettuce builds them (they are combined by
 ``Simulation`` into the per-cell flag byte); the operators themselves run
@@ -21,7 +23,8 @@ from . import _lib
 from ._flow import Boundary
 from ._native import NativeBoundary, NativeCollision
 
-__all__ = ["BounceBackBoundary", "EquilibriumBoundaryPU", "AntiBounceBackOutlet"]
+__all__ = ["BounceBackBoundary", "EquilibriumBoundaryPU", "AntiBounceBackOutlet",
+           "EquilibriumOutletP", "PartiallySaturatedBC"]
 
 
 def _apply_alone(flow, native: NativeBoundary, flags_value):
@@ -164,3 +167,53 @@ class AntiBounceBackOutlet(Boundary):
         axis = [i for i, v in enumerate(self.direction) if v != 0][0]
         return NativeBoundary(_lib.SUB_ANTI_BOUNCE_BACK, index, axis=axis,
                               sign=int(self.direction[axis]))
+
+
+class EquilibriumOutletP(AntiBounceBackOutlet):
+    """pressure outlet: the outlet plane takes feq(rho_outlet, u of the plane
+    one cell inside); only the populations leaving the domain stream into
+    the plane, the others keep the boundary values"""
+
+    def __init__(self, direction: List[int], flow, rho_outlet: float = 1.0):
+        super().__init__(direction, flow)
+        self.context = flow.context
+        self.rho_outlet = self.context.convert_to_tensor(rho_outlet)
+
+    def make_no_streaming_mask(self, shape, context):
+        m = torch.zeros(list(shape), dtype=torch.bool, device=context.device)
+        others = np.setdiff1d(np.arange(shape[0]), self.velocities)
+        m[tuple([others] + self.index)] = True
+        return m
+
+    def native_generator(self, index: int) -> NativeBoundary:
+        axis = [i for i, v in enumerate(self.direction) if v != 0][0]
+        return NativeBoundary(_lib.SUB_EQUILIBRIUM_OUTLET_P, index, axis=axis,
+                              sign=int(self.direction[axis]),
+                              params=(float(self.rho_outlet.item()), 0.0))
+
+
+class PartiallySaturatedBC(Boundary):
+    """partially saturated cells (Noble & Torczynski 1998, Krueger et al.
+    p. 448): a blend of BGK and bounce-back weighted by
+    B = eps (tau - 1/2) / ((1 - eps) + (tau - 1/2)) on the mask"""
+
+    def __init__(self, mask: torch.Tensor, tau: float, saturation: float):
+        self._mask = mask
+        self.tau = tau
+        self.B = saturation * (tau - 0.5) / ((1 - saturation) + (tau - 0.5))
+
+    def __call__(self, flow):
+        return _apply_alone(flow, self.native_generator(1), 1)
+
+    def make_no_collision_mask(self, shape: List[int], context) -> torch.Tensor:
+        return self._mask
+
+    def make_no_streaming_mask(self, shape: List[int], context):
+        return None
+
+    def native_available(self) -> bool:
+        return True
+
+    def native_generator(self, index: int) -> NativeBoundary:
+        return NativeBoundary(_lib.SUB_PARTIALLY_SATURATED, index,
+                              params=(float(self.tau), float(self.B)))

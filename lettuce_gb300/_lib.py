@@ -21,6 +21,7 @@ D1Q3, D2Q9, D3Q15, D3Q19, D3Q27 = 1, 2, 3, 4, 5
 F64, F32, F16_SHIFTED, BF16_SHIFTED = 0, 1, 2, 3
 NO_COLLISION, BGK, TRT, KBC = 0, 1, 2, 3
 SUB_COLLISION, SUB_BOUNCE_BACK, SUB_EQUILIBRIUM_PU, SUB_ANTI_BOUNCE_BACK, SUB_NONE = 0, 1, 2, 3, 4
+SUB_EQUILIBRIUM_OUTLET_P, SUB_PARTIALLY_SATURATED = 5, 6
 PULL, PUSH, LOCAL, AA_EVEN, AA_ODD, STREAM_ONLY, AA_UNPACK = 0, 1, 2, 3, 4, 5, 6
 FLAG_INDEX_MASK, FLAG_NO_STREAM = 0x1F, 0x80
 OPT_ONE_CELL = 1
@@ -39,7 +40,8 @@ class Substep(ctypes.Structure):
                 ("rho", ctypes.c_void_p),
                 ("u", ctypes.c_void_p),
                 ("rho_stride", ctypes.c_int64 * 3),
-                ("u_stride", ctypes.c_int64 * 4)]
+                ("u_stride", ctypes.c_int64 * 4),
+                ("param", ctypes.c_double * 2)]
 
 
 class StepDesc(ctypes.Structure):

@@ -42,6 +42,7 @@ class NativeBoundary:
     index: int
     rho: Optional[torch.Tensor] = None   # equilibrium BC, [1|N1, 1|N2, ...]
     u: Optional[torch.Tensor] = None     # equilibrium BC, [1|D, 1|N1, ...]
-    axis: int = 0                        # anti-bounce-back
+    axis: int = 0                        # outlet-plane substeps
     sign: int = 1
+    params: tuple = (0.0, 0.0)           # pressure outlet (rho,), partially saturated (tau, B)
     keep: list = field(default_factory=list)

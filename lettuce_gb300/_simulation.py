@@ -75,9 +75,11 @@ def _fill_substep(sub: _lib.Substep, native, keep: list, res):
             sub.rho_stride[k] = rs[k] if k < len(rs) else 0
         for k in range(4):
             sub.u_stride[k] = us[k] if k < len(us) else 0
-    elif native.kind == _lib.SUB_ANTI_BOUNCE_BACK:
+    elif native.kind in (_lib.SUB_ANTI_BOUNCE_BACK, _lib.SUB_EQUILIBRIUM_OUTLET_P):
         sub.axis = native.axis
         sub.sign = native.sign
+    for k, v in enumerate(native.params):
+        sub.param[k] = float(v)
 
 
 def _desc_for(flow, natives, flags, nsb, collision_index):

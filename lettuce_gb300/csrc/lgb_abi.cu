@@ -436,7 +436,7 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
         for (int k = 0; k < d->n_sub; ++k) {
             const lgb_substep &s = d->sub[k];
             lgb::SubParams &t = p.sub[k];
-            if (s.kind < LGB_SUB_COLLISION || s.kind > LGB_SUB_NONE)
+            if (s.kind < LGB_SUB_COLLISION || s.kind > LGB_SUB_PARTIALLY_SATURATED)
                 return fail("lgb_step: substep %d has unknown kind %d", k, s.kind);
             if (s.kind == LGB_SUB_COLLISION && k != d->collision_index)
                 return fail("lgb_step: substep %d is a second collision", k);
@@ -451,8 +451,16 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
                     t.us[1 + off + i] = s.u_stride[1 + i];
                 }
             }
-            if (s.kind == LGB_SUB_ANTI_BOUNCE_BACK) {
-                if (p.abb_k >= 0) return fail("lgb_step: more than one anti-bounce-back outlet");
+            if (s.kind == LGB_SUB_PARTIALLY_SATURATED) {
+                if (!(s.param[0] > 0.0))
+                    return fail("lgb_step: partially saturated substep %d needs tau > 0", k);
+                t.param[0] = s.param[0];
+                t.param[1] = s.param[1];
+            }
+            if (s.kind == LGB_SUB_ANTI_BOUNCE_BACK || s.kind == LGB_SUB_EQUILIBRIUM_OUTLET_P) {
+                if (p.abb_k >= 0) return fail("lgb_step: more than one outlet-plane substep");
+                p.abb_kind = s.kind;
+                p.abb_rho = s.param[0];
                 if (s.axis < 0 || s.axis >= g.d || (s.sign != 1 && s.sign != -1))
                     return fail("lgb_step: outlet direction (axis %d, sign %d) invalid", s.axis, s.sign);
                 const int ia = off + s.axis;

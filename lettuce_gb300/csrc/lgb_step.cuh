@@ -57,6 +57,7 @@ struct SubParams {
     const void *u;    // equilibrium BC velocity (compute type)
     int64_t rs[3];    // density strides, internal X, Y, Z
     int64_t us[4];    // velocity strides: component, internal X, Y, Z
+    double param[2];  // partially saturated: tau, B
 };
 
 struct StepParams {
@@ -74,6 +75,8 @@ struct StepParams {
     // neighbour-plane coordinates along that axis
     int32_t abb_k, abb_axis, abb_sign;
     uint32_t abb_plane, abb_nb;
+    int32_t abb_kind;   // LGB_SUB_ANTI_BOUNCE_BACK or LGB_SUB_EQUILIBRIUM_OUTLET_P
+    double abb_rho;     // pressure outlet density
     SubParams sub[LGB_MAX_SUBSTEPS];
     uint32_t *status;
 };
@@ -134,6 +137,7 @@ __device__ __forceinline__ SubParams select_sub(const StepParams &p, int idx) {
     r.kind = LGB_SUB_NONE;
     r.rho = nullptr;
     r.u = nullptr;
+    r.param[0] = r.param[1] = 0.0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) r.rs[d] = 0;
 #pragma unroll
@@ -148,6 +152,8 @@ __device__ __forceinline__ SubParams select_sub(const StepParams &p, int idx) {
             for (int d = 0; d < 3; ++d) r.rs[d] = p.sub[k].rs[d];
 #pragma unroll
             for (int d = 0; d < 4; ++d) r.us[d] = p.sub[k].us[d];
+            r.param[0] = p.sub[k].param[0];
+            r.param[1] = p.sub[k].param[1];
         }
     }
     return r;
@@ -177,6 +183,23 @@ __device__ __forceinline__ void apply_local_substep(const StepParams &p, const S
 #pragma unroll
         for (int d = 0; d < 3; ++d) u[d] = d < S::D ? up[ub + d * sb.us[0]] : R(0);
         set_equilibrium<S>(f, rho, u);
+    } else if (sb.kind == LGB_SUB_PARTIALLY_SATURATED) {
+        // partially_saturated_boundary.py:24-41 (Noble & Torczynski 1998):
+        // f - (1 - B)/tau (f - feq) + B ((f_opp - feq_opp) - (f - feq(rho, 0)))
+        R rho, u[3];
+        cell_moments<S>(f, rho, u);
+        const R uu = dot_uu<S>(u);
+        const R tau = R(sb.param[0]), B = R(sb.param[1]);
+        const R a = (R(1) - B) / tau;
+        R out[S::Q];
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) {
+            const int o = S::opp(q);
+            const R fe = feq_q<S>(q, rho, u, uu), fo = feq_q<S>(o, rho, u, uu);
+            out[q] = f[q] - a * (f[q] - fe) + B * ((f[o] - fo) - (f[q] - R(S::w(q)) * rho));
+        }
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) f[q] = out[q];
     }
 }
 
@@ -184,9 +207,11 @@ __device__ __forceinline__ uint32_t coord_along(const Nbr &c, int axis) {
     return axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
 }
 
-// anti_bounce_back_outlet.py:71-91 at a cell of the outlet plane: the
-// neighbour one cell inside is rebuilt as the collide phase sees it at
-// substep abb_k (its populations after the substeps before abb_k).
+// the outlet-plane substep at a cell of the plane: anti-bounce-back
+// (anti_bounce_back_outlet.py:71-91) or pressure outlet
+// (equilibrium_outlet_p.py:61-71). The neighbour one cell inside is rebuilt
+// as the collide phase sees it at substep abb_k (its populations after the
+// substeps before abb_k).
 template <class S, int COLL, int LOAD, bool MASKED, class Sto>
 __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename Sto::T *__restrict__ fin,
                                              const Nbr &c, typename Sto::R (&f)[S::Q]) {
@@ -203,8 +228,14 @@ __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename
     const int idx = fl & LGB_FLAG_INDEX_MASK;
     if (idx < p.abb_k) apply_local_substep<S, COLL>(p, select_sub(p, idx), cn, g);
     R rho, u[3], rn, un[3];
-    cell_moments<S>(f, rho, u);
     cell_moments<S>(g, rn, un);
+    if (p.abb_kind == LGB_SUB_EQUILIBRIUM_OUTLET_P) {
+        // equilibrium_outlet_p.py:61-71: the plane takes the equilibrium of
+        // the outlet density and the neighbour plane's velocity
+        set_equilibrium<S>(f, R(p.abb_rho), un);
+        return;
+    }
+    cell_moments<S>(f, rho, u);
     R uw[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) uw[d] = u[d] + R(0.5) * (u[d] - un[d]);

@@ -20,6 +20,9 @@
  *   equilibrium BC  lettuce/ext/_boundary/equilibrium_boundary_pu.py:79-84
  *   anti-bounce-back outlet
  *                   lettuce/ext/_boundary/anti_bounce_back_outlet.py:71-91
+ *   pressure outlet lettuce/ext/_boundary/equilibrium_outlet_p.py:61-71
+ *   partially saturated cells
+ *                   lettuce/ext/_boundary/partially_saturated_boundary.py:24-41
  *
  * Parity of this restatement with lettuce itself is pinned by golden
  * vectors generated from lettuce (tests/golden/make_golden.py).
@@ -39,7 +42,8 @@ enum { ORC_D1Q3 = 1, ORC_D2Q9 = 2, ORC_D3Q15 = 3, ORC_D3Q19 = 4, ORC_D3Q27 = 5 }
 enum { ORC_NO_COLLISION = 0, ORC_BGK = 1, ORC_TRT = 2, ORC_KBC = 3 };
 /* substep kinds */
 enum { ORC_SUB_COLLISION = 0, ORC_SUB_BOUNCE_BACK = 1, ORC_SUB_EQUILIBRIUM_PU = 2,
-       ORC_SUB_ANTI_BOUNCE_BACK = 3, ORC_SUB_NONE = 4 };
+       ORC_SUB_ANTI_BOUNCE_BACK = 3, ORC_SUB_NONE = 4, ORC_SUB_EQUILIBRIUM_OUTLET_P = 5,
+       ORC_SUB_PARTIALLY_SATURATED = 6 };
 /* streaming strategies: lettuce's StreamingStrategy enum values
  * (lettuce/cuda_native/_default_code_gen.py:13-17) */
 enum { ORC_NO_STREAMING = 0, ORC_POST_STREAMING = 1, ORC_PRE_STREAMING = 2,
@@ -54,9 +58,11 @@ typedef struct {
     const void *u;
     int64_t rho_stride[3];
     int64_t u_stride[4]; /* [component, x, y, z] */
-    /* anti-bounce-back: lettuce dimension index of the normal and its sign */
+    /* outlet planes: lettuce dimension index of the normal and its sign */
     int32_t axis;
     int32_t sign;
+    /* pressure outlet: [0] = outlet density; partially saturated: tau, B */
+    double param[2];
 } orc_substep;
 
 typedef struct {

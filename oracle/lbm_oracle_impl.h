@@ -260,6 +260,48 @@ static void SFX(anti_bounce_back)(const SFX(geom) *g, const orc_substep *sb, REA
     }
 }
 
+/* pressure outlet, lettuce/ext/_boundary/equilibrium_outlet_p.py:61-71: in
+ * place on the plane, feq(rho_outlet, u of the neighbour plane) */
+static void SFX(equilibrium_outlet_p)(const SFX(geom) *g, const orc_substep *sb, REAL *f)
+{
+    const int D = g->d, Q = g->q, ax = sb->axis;
+    const int64_t n_ax = g->res[ax];
+    const int64_t plane = sb->sign > 0 ? n_ax - 1 : 0;
+    const int64_t nb = sb->sign > 0 ? n_ax - 2 : 1;
+    const int64_t N = g->N;
+    const REAL rho_w = (REAL)sb->param[0];
+    for (int64_t n = 0; n < N; ++n) {
+        int64_t c[3] = {0, 0, 0};
+        SFX(cell_coords)(g, n, c);
+        if (c[ax] != plane) continue;
+        int64_t cn[3] = {c[0], c[1], c[2]};
+        cn[ax] = nb;
+        int64_t m = 0;
+        for (int i = 0; i < D; ++i) m += cn[i] * g->lstride[i];
+        REAL fn[27], rn, un[3], feq[27];
+        for (int q = 0; q < Q; ++q) fn[q] = f[(int64_t)q * N + m];
+        SFX(cell_moments)(g, fn, &rn, un);
+        SFX(cell_feq)(g, rho_w, un, feq);
+        for (int q = 0; q < Q; ++q) f[(int64_t)q * N + n] = feq[q];
+    }
+}
+
+/* partially saturated cell, lettuce/ext/_boundary/partially_saturated_boundary.py:24-41 */
+static void SFX(partially_saturated)(const SFX(geom) *g, const orc_substep *sb, const REAL *fc,
+                                     REAL *out)
+{
+    const int Q = g->q;
+    REAL rho, u[3], feq[27], zero[3] = {0, 0, 0}, feq0[27];
+    SFX(cell_moments)(g, fc, &rho, u);
+    SFX(cell_feq)(g, rho, u, feq);
+    SFX(cell_feq)(g, rho, zero, feq0);
+    const REAL tau = (REAL)sb->param[0], B = (REAL)sb->param[1];
+    for (int q = 0; q < Q; ++q) {
+        const int o = g->st->opp[q];
+        out[q] = fc[q] - (1 - B) / tau * (fc[q] - feq[q]) + B * ((fc[o] - feq[o]) - (fc[q] - feq0[q]));
+    }
+}
+
 /* masked collide: lettuce/_simulation.py:258-305 */
 static void SFX(collide)(const SFX(geom) *g, const orc_problem *p, REAL *f, int nthreads)
 {
@@ -278,6 +320,7 @@ static void SFX(collide)(const SFX(geom) *g, const orc_problem *p, REAL *f, int 
     for (int k = 0; k < p->n_sub; ++k) {
         const orc_substep *sb = &p->sub[k];
         if (sb->kind == ORC_SUB_ANTI_BOUNCE_BACK) { SFX(anti_bounce_back)(g, sb, f); continue; }
+        if (sb->kind == ORC_SUB_EQUILIBRIUM_OUTLET_P) { SFX(equilibrium_outlet_p)(g, sb, f); continue; }
         #pragma omp parallel for num_threads(nthreads) schedule(static)
         for (int64_t n = 0; n < N; ++n) {
             if (p->ncm[n] != k) continue;
@@ -296,6 +339,7 @@ static void SFX(collide)(const SFX(geom) *g, const orc_problem *p, REAL *f, int 
                 SFX(cell_feq)(g, rho, u, out);
                 break;
             }
+            case ORC_SUB_PARTIALLY_SATURATED: SFX(partially_saturated)(g, sb, fc, out); break;
             default: for (int q = 0; q < Q; ++q) out[q] = fc[q]; break;
             }
             for (int q = 0; q < Q; ++q) f[(int64_t)q * N + n] = out[q];

@@ -16,6 +16,10 @@ product's classes:
   lattice units (lettuce/ext/_boundary/equilibrium_boundary_pu.py:71-84)
 * ``{"kind": "anti_bounce_back", "direction": [1, 0, 0]}``
   (lettuce/ext/_boundary/anti_bounce_back_outlet.py:22-103)
+* ``{"kind": "equilibrium_outlet_p", "direction": [1, 0], "rho": 1.0}``
+  (lettuce/ext/_boundary/equilibrium_outlet_p.py:12-91)
+* ``{"kind": "partially_saturated", "mask": bool[*res], "tau": t, "B": b}``
+  (lettuce/ext/_boundary/partially_saturated_boundary.py:6-51)
 """
 from __future__ import annotations
 
@@ -34,7 +38,8 @@ _lib = None
 STENCIL_IDS = {"D1Q3": 1, "D2Q9": 2, "D3Q15": 3, "D3Q19": 4, "D3Q27": 5}
 COLLISION_IDS = {"none": 0, "bgk": 1, "trt": 2, "kbc": 3}
 SUB_KIND = {"collision": 0, "bounce_back": 1, "equilibrium_pu": 2,
-            "anti_bounce_back": 3, "none": 4}
+            "anti_bounce_back": 3, "none": 4, "equilibrium_outlet_p": 5,
+            "partially_saturated": 6}
 # lettuce/cuda_native/_default_code_gen.py:13-17
 STRATEGY_IDS = {"NO_STREAMING": 0, "POST_STREAMING": 1, "PRE_STREAMING": 2,
                 "DOUBLE_STREAMING": 3}
@@ -79,7 +84,8 @@ class _Sub(ctypes.Structure):
                 ("rho_stride", ctypes.c_int64 * 3),
                 ("u_stride", ctypes.c_int64 * 4),
                 ("axis", ctypes.c_int32),
-                ("sign", ctypes.c_int32)]
+                ("sign", ctypes.c_int32),
+                ("param", ctypes.c_double * 2)]
 
 
 class _Problem(ctypes.Structure):
@@ -140,8 +146,19 @@ def boundary_masks(b, resolution, q, name):
     the boundaries' make_no_collision_mask / make_no_streaming_mask."""
     res = list(resolution)
     kind = b["kind"]
-    if kind in ("bounce_back", "equilibrium_pu"):
+    if kind in ("bounce_back", "equilibrium_pu", "partially_saturated"):
         return np.asarray(b["mask"], dtype=bool), None
+    if kind == "equilibrium_outlet_p":
+        # lettuce/ext/_boundary/equilibrium_outlet_p.py:73-85
+        e, _, _ = stencil_tables(name)
+        direction = list(b["direction"])
+        vel = np.where(e @ np.array(direction) > 1 - 1e-6)[0]
+        index = [slice(None) if i == 0 else (-1 if i == 1 else 0) for i in direction]
+        nsm = np.zeros([q] + res, dtype=bool)
+        nsm[tuple([np.setdiff1d(np.arange(q), vel)] + index)] = True
+        ncm = np.zeros(res, dtype=bool)
+        ncm[tuple(index)] = True
+        return ncm, nsm
     if kind == "anti_bounce_back":
         # lettuce/ext/_boundary/anti_bounce_back_outlet.py:37-58, 93-103
         e, _, opp = stencil_tables(name)
@@ -219,11 +236,16 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
                 s.rho_stride[k] = rs[k] if k < len(rs) else 0
             for k in range(4):
                 s.u_stride[k] = us[k] if k < len(us) else 0
-        if b["kind"] == "anti_bounce_back":
+        if b["kind"] in ("anti_bounce_back", "equilibrium_outlet_p"):
             d = list(b["direction"])
             ax = [i for i, v in enumerate(d) if v != 0][0]
             s.axis = ax
             s.sign = int(d[ax])
+        if b["kind"] == "equilibrium_outlet_p":
+            s.param[0] = float(b.get("rho", 1.0))
+        if b["kind"] == "partially_saturated":
+            s.param[0] = float(b["tau"])
+            s.param[1] = float(b["B"])
     p = _Problem()
     p.stencil = STENCIL_IDS[name]
     for k in range(3):

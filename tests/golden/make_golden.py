@@ -23,8 +23,9 @@ warnings.filterwarnings("ignore")
 import lettuce as lt  # noqa: E402
 from lettuce import (Context, Simulation, StreamingStrategy,  # noqa: E402
                      UnitConversion)
+from lettuce.ext._boundary.partially_saturated_boundary import PartiallySaturatedBC  # noqa: E402
 from lettuce.ext import (D1Q3, D2Q9, D3Q15, D3Q19, D3Q27,  # noqa: E402
-                         AntiBounceBackOutlet, BGKCollision,
+                         AntiBounceBackOutlet, BGKCollision, EquilibriumOutletP,
                          BounceBackBoundary, EquilibriumBoundaryPU, ExtFlow,
                          IncompressibleKineticEnergy, KBCCollision,
                          MaximumVelocity, NoCollision, Obstacle,
@@ -155,6 +156,68 @@ def case_obstacle(name, stencil, res, radius, coll, steps):
                               "radius": radius, "collision": coll,
                               "stencil": stencil.__name__, "re": 100,
                               "ma": 0.1, "domain_length_x": res[0] / 4.0})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_outlet_p(name, stencil, res, radius, rho_outlet, steps):
+    """an obstacle flow whose outlet is lettuce's pressure outlet
+    (EquilibriumOutletP, left commented out in obstacle.py:119-120)"""
+    class ObstacleP(Obstacle):
+        @property
+        def post_boundaries(self):
+            b = Obstacle.post_boundaries.fget(self)
+            return [b[0], EquilibriumOutletP(self._unit_vector().tolist(), self,
+                                             rho_outlet=rho_outlet), b[2]]
+    out = {}
+    for sname, strat in STRATS.items():
+        flow = ObstacleP(CTX, resolution=res, reynolds_number=100, mach_number=0.1,
+                         domain_length_x=res[0] / 4.0, stencil=stencil)
+        grid = np.meshgrid(*[np.arange(n) for n in res], indexing="ij")
+        centre = [res[0] / 3.0] + [n / 2.0 - 0.5 for n in res[1:]]
+        mask = sum((g - c) ** 2 for g, c in zip(grid, centre)) < radius ** 2
+        flow.mask = mask
+        flow.initialize()
+        out["f0"] = npf(flow.f)
+        tau = flow.units.relaxation_parameter_lu
+        sim = Simulation(flow, BGKCollision(tau), [], streaming_strategy=strat)
+        out["ncm"] = npf(sim.no_collision_mask).astype(np.uint8)
+        out["nsm"] = npf(sim.no_streaming_mask).astype(np.uint8)
+        sim(steps)
+        out["mask"] = mask
+        out[f"f_{sname}"] = npf(flow.f)
+        out["tau"] = np.float64(tau)
+        inlet = flow.post_boundaries[0]
+        out["inlet_u_lu"] = npf(flow.units.convert_velocity_to_lu(inlet.velocity))
+        out["inlet_rho_lu"] = npf(flow.units.convert_pressure_pu_to_density_lu(
+            inlet.pressure))
+    out["steps"] = np.int64(steps)
+    out["meta"] = json.dumps({"flow": "ObstacleP", "res": res, "radius": radius,
+                              "collision": "bgk", "stencil": stencil.__name__, "re": 100,
+                              "ma": 0.1, "domain_length_x": res[0] / 4.0,
+                              "rho_outlet": rho_outlet})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_psm(name, stencil, res, saturation, steps, seed):
+    """partially saturated cells (Noble-Torczynski) on a block of cells"""
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.05 * rng.standard_normal([st.q] + res))
+    mask = np.zeros(res, dtype=bool)
+    mask[tuple(slice(n // 4, n // 4 + max(2, n // 3)) for n in res)] = True
+    tau = 0.7
+    out = {"f0": f0, "mask": mask, "tau": np.float64(tau), "steps": np.int64(steps),
+           "saturation": np.float64(saturation)}
+    for sname, strat in STRATS.items():
+        flow = GivenFlow(st, f0)
+        b = PartiallySaturatedBC(torch.tensor(mask), tau, saturation)
+        flow.bnds = [b]
+        out["B"] = np.float64(b.B)
+        sim = Simulation(flow, BGKCollision(tau), [], streaming_strategy=strat)
+        sim(steps)
+        out[f"f_{sname}"] = npf(flow.f)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res, "collision": "bgk"})
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
 
 
@@ -306,6 +369,10 @@ def main():
     case_obstacle("obstacle2d_d2q9_bgk", D2Q9, [32, 16], 3.0, "bgk", 10)
     case_obstacle("obstacle3d_d3q27_kbc", D3Q27, [24, 8, 8], 2.0, "kbc", 3)
     case_eqpu_field("eqpu_field_d2q9")
+    case_outlet_p("outletp_d2q9_bgk", D2Q9, [32, 16], 3.0, 1.0, 10)
+    case_outlet_p("outletp_d3q19_bgk", D3Q19, [20, 8, 8], 2.0, 1.01, 4)
+    case_psm("psm_d2q9_bgk", D2Q9, [20, 16], 0.4, 5, 21)
+    case_psm("psm_d3q19_bgk", D3Q19, [9, 8, 7], 0.7, 3, 22)
     case_native_kats()
     case_observables()
     case_adjoint()

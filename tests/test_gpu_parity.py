@@ -301,3 +301,52 @@ def test_shifted_storage_matches_f32_closely(lgb, oracle):
     w = np.array(lt.D2Q9().w).reshape(-1, 1, 1)
     hmax = np.max(np.abs(ref - w))
     assert np.max(np.abs(to_np(flow.f) - ref)) < 20 * hmax * 2.0 ** -11
+
+
+class _ObstacleP(lt.Obstacle):
+    """an obstacle flow with lettuce's pressure outlet instead of the
+    anti-bounce-back outlet"""
+    rho_outlet = 1.0
+
+    @property
+    def post_boundaries(self):
+        b = lt.Obstacle.post_boundaries.fget(self)
+        return [b[0], lt.EquilibriumOutletP(self._unit_vector().tolist(), self,
+                                            rho_outlet=self.rho_outlet), b[2]]
+
+
+@pytest.mark.parametrize("name", golden_names("outletp"))
+@pytest.mark.parametrize("strategy", list(STRATS))
+@pytest.mark.parametrize("dtype", [F64, F32])
+def test_pressure_outlet_matches_lettuce(lgb, name, strategy, dtype):
+    z = golden(name)
+    m = meta(z)
+    S = getattr(lt, m["stencil"])
+    _ObstacleP.rho_outlet = m["rho_outlet"]
+    flow = _ObstacleP(ctx(dtype), m["res"], m["re"], m["ma"], m["domain_length_x"], stencil=S)
+    flow.mask = z["mask"]
+    flow.initialize()
+    sim = lt.Simulation(flow, lt.BGKCollision(flow.units.relaxation_parameter_lu), [],
+                        streaming_strategy=STRATS[strategy])
+    assert np.array_equal(to_np(sim.no_collision_mask), z["ncm"])
+    assert np.array_equal(to_np(sim.no_streaming_mask), z["nsm"])
+    sim(int(z["steps"]))
+    assert rel_max(to_np(flow.f), z[f"f_{strategy}"]) < tol(dtype, "bgk", int(z["steps"]))
+
+
+@pytest.mark.parametrize("name", golden_names("psm"))
+@pytest.mark.parametrize("strategy", list(STRATS))
+@pytest.mark.parametrize("dtype", [F64, F32])
+def test_partially_saturated_matches_lettuce(lgb, name, strategy, dtype):
+    z = golden(name)
+    m = meta(z)
+    S = getattr(lt, m["stencil"])
+    flow = GivenFlow(ctx(dtype), S(), z["f0"])
+    b = lt.PartiallySaturatedBC(torch.tensor(z["mask"]).cuda(), float(z["tau"]),
+                                float(z["saturation"]))
+    assert abs(b.B - float(z["B"])) < 1e-15
+    flow._bnds = [b]
+    sim = lt.Simulation(flow, lt.BGKCollision(float(z["tau"])), [],
+                        streaming_strategy=STRATS[strategy])
+    sim(int(z["steps"]))
+    assert rel_max(to_np(flow.f), z[f"f_{strategy}"]) < tol(dtype, "bgk", int(z["steps"]))

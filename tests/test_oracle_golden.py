@@ -101,3 +101,40 @@ def test_oracle_energy_decay_series(oracle):
     dx = flow.units.convert_length_to_pu(1.0)
     k = flow.units.convert_incompressible_energy_to_pu(oracle.kinetic_energy("D2Q9", f100))
     assert abs(k * dx ** 2 / e["energy"][1] - 1) < 1e-12
+
+
+def outletp_boundaries(z, m):
+    res = m["res"]
+    d = len(res)
+    x = np.arange(res[0]).reshape([-1] + [1] * (d - 1)) * np.ones(res)
+    return [{"kind": "equilibrium_pu", "mask": np.abs(x) < 1e-6,
+             "rho": z["inlet_rho_lu"].reshape([1] * d),
+             "u": z["inlet_u_lu"].reshape([d] + [1] * d)},
+            {"kind": "equilibrium_outlet_p", "direction": [1] + [0] * (d - 1),
+             "rho": m["rho_outlet"]},
+            {"kind": "bounce_back", "mask": z["mask"]}]
+
+
+@pytest.mark.parametrize("name", golden_names("outletp"))
+@pytest.mark.parametrize("strategy", STRATS)
+def test_pressure_outlet_cases(oracle, name, strategy):
+    z = golden(name)
+    m = meta(z)
+    post = outletp_boundaries(z, m)
+    ncm, nsm = oracle.assemble_masks(m["res"], z["f0"].shape[0], m["stencil"], [], post)
+    assert np.array_equal(ncm, z["ncm"]) and np.array_equal(nsm, z["nsm"])
+    out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision="bgk",
+                     tau=float(z["tau"]), strategy=strategy, post=post)
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", golden_names("psm"))
+@pytest.mark.parametrize("strategy", STRATS)
+def test_partially_saturated_cases(oracle, name, strategy):
+    z = golden(name)
+    m = meta(z)
+    post = [{"kind": "partially_saturated", "mask": z["mask"], "tau": float(z["tau"]),
+             "B": float(z["B"])}]
+    out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision="bgk",
+                     tau=float(z["tau"]), strategy=strategy, post=post)
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
