@@ -82,10 +82,12 @@ def _fill_substep(sub: _lib.Substep, native, keep: list, res):
         sub.param[k] = float(v)
 
 
-def _desc_for(flow, natives, flags, nsb, collision_index):
-    """lgb_step_desc for a list of substep descriptors (collision included)"""
+def _desc_for(flow, natives, flags, nsb, collision_index, res=None):
+    """lgb_step_desc for a list of substep descriptors (collision included);
+    ``res`` overrides the flow's resolution (a slab of the grid)"""
     coll = natives[collision_index]
-    d = _device.new_desc(flow.stencil.lgb_id, flow.context.storage, flow.resolution)
+    res = list(flow.resolution if res is None else res)
+    d = _device.new_desc(flow.stencil.lgb_id, flow.context.storage, res)
     d.collision = coll.kind
     d.tau = coll.tau
     d.tau_minus = coll.tau_minus
@@ -98,7 +100,7 @@ def _desc_for(flow, natives, flags, nsb, collision_index):
         d.n_sub = len(natives)
         d.collision_index = collision_index
         for k, nat in enumerate(natives):
-            _fill_substep(d.sub[k], nat, keep, flow.resolution)
+            _fill_substep(d.sub[k], nat, keep, res)
     return d, keep
 
 
@@ -153,9 +155,20 @@ def apply_local(flow, collision_native: NativeCollision,
 
 
 class Simulation:
+    """lettuce's Simulation on the GB300 kernels.
+
+    ``memory_pattern``: "ab" (two fields) or "aa" (in place, POST_STREAMING).
+    ``use_graph``: replay pairs of steps from a captured CUDA graph instead of
+    launching every step from Python. ``None`` (default) enables it when the
+    simulation has no reporters; with reporters and ``use_graph=True`` the
+    reporters are called at the steps where one of them is due
+    (``flow.i % interval == 0``) instead of after every step."""
+
     def __init__(self, flow, collision, reporter: List[Reporter],
                  streaming_strategy=StreamingStrategy.POST_STREAMING,
-                 memory_pattern: str = "ab"):
+                 memory_pattern: str = "ab", use_graph: Optional[bool] = None):
+        self.use_graph = use_graph
+        self._graph = None
         self.flow = flow
         flow.collision = collision
         self.context = flow.context
@@ -264,6 +277,77 @@ class Simulation:
             _device.step(d, stream)
             flow._f, flow._f_next = dst, src
 
+    # -- CUDA-graph replay -------------------------------------------------
+    def _graphs_enabled(self) -> bool:
+        if self.use_graph is None:
+            return not self.reporter
+        return bool(self.use_graph)
+
+    def _state_key(self):
+        import ctypes
+        d = self._desc
+        return (self.flow._f.data_ptr(),
+                self.flow._f_next.data_ptr() if self.flow._f_next is not None else 0,
+                self.flow._aa_pending,
+                ctypes.string_at(ctypes.addressof(d), ctypes.sizeof(d)))
+
+    def _advance(self, n: int):
+        """n steps without reporters; flow.i is advanced"""
+        flow = self.flow
+        if not self._graphs_enabled() or n < 4:
+            for _ in range(n):
+                self._collide_and_stream(self)
+                flow.i += 1
+            return
+        if self.memory_pattern != "aa":
+            flow.f_next  # make sure the second field exists before capture
+        if self._graph is None:
+            self._graph = {}
+        g = self._graph.get(self._state_key())
+        if g is None:
+            # two eager steps (they count), then capture a pair of steps that
+            # returns the fields to the same assignment; graphs are kept per
+            # field assignment (both parities of A/B, both AA phases)
+            for _ in range(2):
+                self._collide_and_stream(self)
+                flow.i += 1
+            n -= 2
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._collide_and_stream(self)
+                self._collide_and_stream(self)
+            if len(self._graph) >= 4:
+                self._graph.clear()
+            self._graph[self._state_key()] = g
+        for _ in range(n // 2):
+            g.replay()
+        flow.i += 2 * (n // 2)
+        for _ in range(n % 2):
+            self._collide_and_stream(self)
+            flow.i += 1
+
+    def _steps_to_next_report(self) -> int:
+        i = self.flow.i
+        best = None
+        for r in self.reporter:
+            iv = int(getattr(r, "interval", 1) or 1)
+            k = iv - (i % iv)
+            best = k if best is None else min(best, k)
+        return best if best is not None else 1 << 62
+
+    def _run(self, target_done):
+        """advance until target_done() holds, reporting like lettuce"""
+        graphs = self._graphs_enabled()
+        while not target_done():
+            if not graphs:
+                self._collide_and_stream(self)
+                self.flow.i += 1
+                self._report()
+                continue
+            m = min(self._steps_to_next_report(), self._remaining())
+            self._advance(m)
+            self._report()
+
     def step(self, num_steps: int):
         warnings.warn("Simulation.step() is deprecated; call simulation(num_steps)",
                       DeprecationWarning)
@@ -278,10 +362,9 @@ class Simulation:
         beg = timer()
         if self.flow.i == 0:
             self._report()
-        for _ in range(num_steps):
-            self._collide_and_stream(self)
-            self.flow.i += 1
-            self._report()
+        stop = self.flow.i + num_steps
+        self._remaining = lambda: stop - self.flow.i
+        self._run(lambda: self.flow.i >= stop)
         self.context.synchronize()
         end = timer()
         return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)
@@ -299,10 +382,8 @@ class BreakableSimulation(Simulation):
         beg = timer()
         if self.flow.i == 0:
             self._report()
-        while self.flow.i < num_steps:
-            self._collide_and_stream(self)
-            self.flow.i += 1
-            self._report()
+        self._remaining = lambda: max(1, num_steps - self.flow.i)
+        self._run(lambda: self.flow.i >= num_steps)
         self.context.synchronize()
         end = timer()
         return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)
