@@ -24,6 +24,7 @@ from ._flows import ExtFlow, Obstacle, TaylorGreenVortex
 from ._native import NativeBoundary, NativeCollision, NativeEquilibrium
 from ._batched import BatchedSimulation, batched_taylor_green
 from ._adjoint import moments_torch, rollout
+from ._slab import Slab, SlabSimulation, exchange, exchange_local
 
 __version__ = "0.1.0"
 
@@ -39,5 +40,6 @@ __all__ = [
     "Enstrophy", "EnergySpectrum", "Mass", "ErrorReporter", "FailureReporterBase",
     "NaNReporter", "HighMaReporter", "ExtFlow", "TaylorGreenVortex", "Obstacle",
     "NativeBoundary", "NativeCollision", "NativeEquilibrium", "BatchedSimulation",
-    "batched_taylor_green", "rollout", "moments_torch",
+    "batched_taylor_green", "rollout", "moments_torch", "Slab", "SlabSimulation",
+    "exchange", "exchange_local",
 ]
