@@ -62,8 +62,11 @@ enum {
 };
 
 /* per-cell flag byte: low 5 bits = substep index (lettuce's
- * no_collision_mask value); bit 7 = the cell has no-streaming bits */
+ * no_collision_mask value); bit 7 = the cell has no-streaming bits; bit 6 =
+ * some neighbour x + e_q does not stream population q (read only under
+ * LGB_OPT_PUSH_GUARD) */
 #define LGB_FLAG_INDEX_MASK 0x1f
+#define LGB_FLAG_PUSH_GUARD 0x40
 #define LGB_FLAG_NO_STREAM 0x80
 
 typedef struct {
@@ -108,6 +111,10 @@ typedef struct {
 /* options: run the one-cell-per-thread kernel even where the two-cell
  * kernel of the 16-bit formats applies (results are bit-identical) */
 #define LGB_OPT_ONE_CELL 1
+/* the flags carry LGB_FLAG_PUSH_GUARD: in the PUSH pattern a cell reads its
+ * destinations' no-streaming bits only when its own guard bit is set (without
+ * this option every cell reads them for every population) */
+#define LGB_OPT_PUSH_GUARD 2
 
 /* ABI version of the loaded library */
 int lgb_abi_version(void);

@@ -23,8 +23,8 @@ NO_COLLISION, BGK, TRT, KBC = 0, 1, 2, 3
 SUB_COLLISION, SUB_BOUNCE_BACK, SUB_EQUILIBRIUM_PU, SUB_ANTI_BOUNCE_BACK, SUB_NONE = 0, 1, 2, 3, 4
 SUB_EQUILIBRIUM_OUTLET_P, SUB_PARTIALLY_SATURATED = 5, 6
 PULL, PUSH, LOCAL, AA_EVEN, AA_ODD, STREAM_ONLY, AA_UNPACK = 0, 1, 2, 3, 4, 5, 6
-FLAG_INDEX_MASK, FLAG_NO_STREAM = 0x1F, 0x80
-OPT_ONE_CELL = 1
+FLAG_INDEX_MASK, FLAG_PUSH_GUARD, FLAG_NO_STREAM = 0x1F, 0x40, 0x80
+OPT_ONE_CELL, OPT_PUSH_GUARD = 1, 2
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
             "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_reduce_static", "lgb_convert",

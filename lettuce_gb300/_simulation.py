@@ -21,7 +21,7 @@ from abc import ABC, abstractmethod
 from enum import Enum
 from functools import lru_cache
 from timeit import default_timer as timer
-from typing import List, Optional
+from typing import List, Optional, Sequence
 
 import torch
 
@@ -104,13 +104,16 @@ def _desc_for(flow, natives, flags, nsb, collision_index, res=None):
     return d, keep
 
 
-def pack_masks(no_collision_mask: torch.Tensor, no_streaming_mask: torch.Tensor):
+def pack_masks(no_collision_mask: torch.Tensor, no_streaming_mask: torch.Tensor,
+               e: Optional[Sequence[Sequence[int]]] = None):
     """(flags uint8 [*res], no-stream bits int32 [*res] or None).
 
     flags = the no-collision index | 0x80 where the cell has any population
     that does not stream; bit q of the word is set where lettuce's torch
     stream keeps population q (``no_streaming_mask[q] == 1``,
-    lettuce/_simulation.py:254-255)."""
+    lettuce/_simulation.py:254-255). With the stencil's velocities ``e``,
+    0x40 marks the cells x whose neighbour x + e_q keeps population q (the
+    cells that must look before they push)."""
     ncm = no_collision_mask.to(torch.uint8)
     if int(ncm.max().item()) > _lib.FLAG_INDEX_MASK:
         raise ValueError("too many substeps for the flag byte")
@@ -124,6 +127,13 @@ def pack_masks(no_collision_mask: torch.Tensor, no_streaming_mask: torch.Tensor)
     flags = ncm | (has.to(torch.uint8) * _lib.FLAG_NO_STREAM)
     if not bool(has.any().item()):
         return flags.contiguous(), None
+    if e is not None:
+        d = keep.dim() - 1
+        guard = torch.zeros_like(has)
+        for qi in range(1, q):
+            shift = tuple(-int(v) for v in e[qi])
+            guard |= torch.roll(keep[qi], shifts=shift, dims=tuple(range(d)))
+        flags |= guard.to(torch.uint8) * _lib.FLAG_PUSH_GUARD
     return flags.contiguous(), bits.to(torch.int32).contiguous()
 
 
@@ -219,9 +229,12 @@ class Simulation:
 
         self._flags = self._nsb = None
         if self.no_collision_mask is not None:
-            self._flags, self._nsb = pack_masks(self.no_collision_mask, self.no_streaming_mask)
+            self._flags, self._nsb = pack_masks(self.no_collision_mask, self.no_streaming_mask,
+                                                e=flow.stencil.e)
         self._desc, self._keep = _desc_for(flow, natives, self._flags, self._nsb,
                                            self.collision_index)
+        if self._nsb is not None:
+            self._desc.options |= _lib.OPT_PUSH_GUARD
         self._status = None
         if self.context.device.type == "cuda":
             self._status = torch.zeros(1, dtype=torch.int32, device=self.context.device)

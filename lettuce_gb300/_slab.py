@@ -34,6 +34,7 @@ import numpy as np
 import torch
 
 from . import _device, _lib
+from ._native import NativeBoundary
 
 __all__ = ["Slab", "exchange", "exchange_local", "SlabSimulation"]
 
@@ -159,8 +160,8 @@ class SlabSimulation:
         if sim.memory_pattern == "aa":
             raise ValueError("the AA pattern is not decomposed into slabs")
         for nat in sim._natives:
-            if getattr(nat, "kind", None) in (_lib.SUB_ANTI_BOUNCE_BACK,
-                                              _lib.SUB_EQUILIBRIUM_OUTLET_P):
+            if isinstance(nat, NativeBoundary) and nat.kind in (_lib.SUB_ANTI_BOUNCE_BACK,
+                                                                _lib.SUB_EQUILIBRIUM_OUTLET_P):
                 raise ValueError("outlet planes are not decomposed into slabs")
         if _lib.PUSH in sim._patterns and sim._nsb is not None:
             raise ValueError("push steps with populations that do not stream are "
@@ -195,6 +196,7 @@ class SlabSimulation:
             d.tau = sim._desc.tau
             d.tau_minus = sim._desc.tau_minus
             d.status = self._status.data_ptr()
+            d.options = sim._desc.options
             self._keep += [flags, nsb, natives, keep]
             self._descs.append(d)
         self.i = flow.i
@@ -202,7 +204,7 @@ class SlabSimulation:
     def _slab_native(self, nat, slab: Slab):
         """a substep descriptor with its per-cell tensors cut to the slab"""
         import copy
-        if getattr(nat, "kind", None) != _lib.SUB_EQUILIBRIUM_PU:
+        if not isinstance(nat, NativeBoundary) or nat.kind != _lib.SUB_EQUILIBRIUM_PU:
             return nat
         nat = copy.copy(nat)
         nat.rho = slab.extend(nat.rho, 0).to(self.device)

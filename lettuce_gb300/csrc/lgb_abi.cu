@@ -385,6 +385,8 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (!d) return fail("lgb_step: descriptor is NULL");
     if (d->abi_version != LGB_ABI_VERSION)
         return fail("lgb_step: descriptor ABI version %d, library %d", d->abi_version, LGB_ABI_VERSION);
+    if (d->options & ~(LGB_OPT_ONE_CELL | LGB_OPT_PUSH_GUARD))
+        return fail("lgb_step: unknown option bits 0x%x", (unsigned)d->options);
     Grid g;
     if (make_grid(d->stencil, d->res, &g)) return -1;
     if (!valid_storage(d->storage)) return fail("lgb_step: unknown storage id %d", d->storage);
@@ -429,6 +431,7 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
         p.flags = d->flags;
         p.nsb = d->no_stream_bits;
         p.has_nsm = d->no_stream_bits != nullptr;
+        p.push_guard = (d->options & LGB_OPT_PUSH_GUARD) != 0;
         if (p.has_nsm && (d->pattern == LGB_AA_EVEN || d->pattern == LGB_AA_ODD))
             return fail("lgb_step: no-streaming masks are not supported by the AA pattern");
         p.n_sub = d->n_sub;

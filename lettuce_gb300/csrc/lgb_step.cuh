@@ -69,6 +69,7 @@ struct StepParams {
     const uint8_t *flags;
     const uint32_t *nsb;
     int32_t has_nsm;
+    int32_t push_guard;  // the flags carry LGB_FLAG_PUSH_GUARD
     int32_t n_sub;
     // the anti-bounce-back outlet (at most one): its substep index (-1 for
     // none), internal axis of its normal (0=X, 1=Y, 2=Z), sign, plane and
@@ -347,6 +348,12 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     }
 
     const size_t N = p.N;
+    // PUSH with no-streaming bits: this cell keeps some of its own values or
+    // writes into a destination that keeps some of its own
+    bool guarded = false;
+    if constexpr (MASKED && PAT == LGB_PUSH)
+        guarded = p.has_nsm &&
+                  (!p.push_guard || (fl & (LGB_FLAG_PUSH_GUARD | LGB_FLAG_NO_STREAM)));
 #pragma unroll
     for (int q = 0; q < S::Q; ++q) {
         if constexpr (PAT == LGB_PULL || PAT == LGB_LOCAL || PAT == LGB_STREAM_ONLY ||
@@ -356,7 +363,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
             store_value<Sto, HSPACE>(fout + (size_t)S::opp(q) * N + n, f[q], S::w(q));
         } else {  // PUSH, AA_ODD: to the neighbour in direction e_q, slot q
             const uint32_t dst = c.at(ix<S>(q), iy<S>(q), iz<S>(q), p);
-            if (MASKED && PAT == LGB_PUSH && p.has_nsm && q != 0) {
+            if (MASKED && PAT == LGB_PUSH && guarded && q != 0) {
                 // lettuce keeps the destination's own value where its
                 // no-streaming bit is set
                 const uint8_t fd = p.flags[dst];

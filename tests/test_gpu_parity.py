@@ -350,3 +350,31 @@ def test_partially_saturated_matches_lettuce(lgb, name, strategy, dtype):
                         streaming_strategy=STRATS[strategy])
     sim(int(z["steps"]))
     assert rel_max(to_np(flow.f), z[f"f_{strategy}"]) < tol(dtype, "bgk", int(z["steps"]))
+
+
+@pytest.mark.parametrize("name", golden_names("obstacle") + golden_names("outletp"))
+def test_push_guard_bit_identical(lgb, name):
+    """the push-guard flag bit (only cells next to a non-streaming population
+    look at their destinations' bits) changes no result"""
+    z = golden(name)
+    m = meta(z)
+    outs = []
+    for guard in (True, False):
+        if name.startswith("outletp"):
+            _ObstacleP.rho_outlet = m["rho_outlet"]
+            flow = _ObstacleP(ctx(F64), m["res"], m["re"], m["ma"], m["domain_length_x"],
+                              stencil=getattr(lt, m["stencil"]))
+            flow.mask = z["mask"]
+            flow.initialize()
+        else:
+            flow = obstacle_flow(ctx(F64), z, m)
+        coll = lt.KBCCollision() if m["collision"] == "kbc" else \
+            lt.BGKCollision(flow.units.relaxation_parameter_lu)
+        sim = lt.Simulation(flow, coll, [], streaming_strategy=lt.StreamingStrategy.POST_STREAMING)
+        from lettuce_gb300 import _lib
+        assert sim._desc.options & _lib.OPT_PUSH_GUARD
+        if not guard:
+            sim._desc.options &= ~_lib.OPT_PUSH_GUARD
+        sim(7)
+        outs.append(flow.f_raw.clone())
+    assert torch.equal(outs[0], outs[1])

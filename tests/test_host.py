@@ -97,6 +97,16 @@ def test_pack_masks_bits():
     assert np.array_equal((flags & _lib.FLAG_NO_STREAM) != 0, keep.any(axis=0))
     # outlet plane: the populations entering from +x do not stream
     assert keep[:, -1].sum() == 9 * 8 * 8
+    # push guard: x is marked where some x + e_q keeps population q
+    e = np.asarray(flow.stencil.e)
+    res = flow.resolution
+    guard = np.zeros(res, dtype=bool)
+    for x in np.ndindex(*res):
+        for k in range(1, q):
+            dst = tuple((np.asarray(x) + e[k]) % res)
+            guard[x] |= keep[k][dst]
+    assert np.array_equal((flags & _lib.FLAG_PUSH_GUARD) != 0, guard)
+    assert sim._desc.options & _lib.OPT_PUSH_GUARD
 
 
 def test_pack_masks_collision_index_quirk():
