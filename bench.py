@@ -6,7 +6,9 @@ one pull-pattern pass (lettuce PRE_STREAMING, the CLI benchmark default).
 Populations stored as float32 (headline ``value``) and as shifted float16
 with float32 arithmetic (``fp16_shifted``); the in-place AA variants are
 reported beside them. The 16-bit run's velocity error against a float64 run
-of the same 1000 steps is measured in ``accuracy``.
+of the same 1000 steps is measured in ``accuracy``. ``configs`` holds short
+timed runs of the other configurations of the family (D3Q27 KBC obstacle,
+256 batched D2Q9 domains, the D2Q9 adjoint); ``--no-configs`` skips them.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -275,6 +277,123 @@ def accuracy_fp16(lt, torch, device, steps=1000):
     return out
 
 
+def _event_ms(torch, fn, steps, warmup, device):
+    """mean milliseconds of fn() from CUDA events on the current stream"""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize(device)
+    stream = torch.cuda.current_stream(device)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    end.record(stream)
+    torch.cuda.synchronize(device)
+    return start.elapsed_time(end) / steps
+
+
+def measure_configs(lt, torch, device, peak):
+    """the other configurations of the workload family, each at full size
+    with a short timed run (CUDA events, inputs larger than L2):
+    config 3: D3Q27 KBC obstacle 512x128x128 (sphere d=24 at x=128,
+    equilibrium inlet, anti-bounce-back outlet, Re 300, u_lu 0.05), float32,
+    PRE and POST streaming; config 4: 256 periodic D2Q9 TRT Taylor-Green
+    domains with sides drawn from [32, 512] (numpy default_rng(0)), float32
+    and fp16-shifted, one persistent launch per step replayed from a CUDA
+    graph; config 5: D2Q9 BGK 512^2, float32, 200 steps, gradient of
+    MSE(u(200), target) w.r.t. u0 through the hand-written adjoint with a
+    checkpoint every 20 steps."""
+    import math
+    out = {}
+    res = [512, 128, 128]
+    n = int(np.prod(res))
+    flow = lt.Obstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                       512 / 24, stencil=lt.D3Q27)
+    g = [torch.arange(k, device=device, dtype=torch.float32) for k in res]
+    X, Y, Z = torch.meshgrid(*g, indexing="ij")
+    flow.mask = ((X - 128.0) ** 2 + (Y - 63.5) ** 2 + (Z - 63.5) ** 2) < 144
+    del X, Y, Z
+    flow.initialize()
+    c3 = {"workload": "D3Q27 KBC obstacle 512x128x128, float32", "bytes_per_cell": 217}
+    for strat in ("PRE_STREAMING", "POST_STREAMING"):
+        sim = lt.Simulation(flow, lt.KBCCollision(), [],
+                            streaming_strategy=getattr(lt.StreamingStrategy, strat))
+        ms = _event_ms(torch, sim._collide_and_stream, 100, 10, device)
+        gbs = 217 * n / (ms * 1e-3) / 1e9
+        c3[strat] = {"mlups": round(n / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms, 4),
+                     "achieved_gbs": round(gbs, 1), "frac_of_peak": round(gbs / peak, 4)}
+        del sim
+    del flow, g
+    torch.cuda.empty_cache()
+    out["config3_kbc_obstacle"] = c3
+
+    c4 = {"workload": "256 D2Q9 TRT Taylor-Green domains, sides in [32, 512], Re in [100, 5000]"}
+    for storage in (None, "fp16_shifted"):
+        flows, colls = lt.batched_taylor_green(lt.Context(device, torch.float32, storage=storage),
+                                               256, seed=0)
+        sim = lt.BatchedSimulation(flows, colls)
+        sim(4)
+        torch.cuda.synchronize(device)
+        steps = 200
+        stream = torch.cuda.current_stream(device)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        sim.advance(steps)
+        end.record(stream)
+        torch.cuda.synchronize(device)
+        ms = start.elapsed_time(end) / steps
+        bpc = 2 * 9 * (2 if storage else 4)
+        gbs = bpc * sim.n_cells / (ms * 1e-3) / 1e9
+        c4[storage or "float32"] = {
+            "cells": sim.n_cells, "mlups": round(sim.n_cells / (ms * 1e-3) / 1e6, 1),
+            "ms_per_step": round(ms, 4), "achieved_gbs": round(gbs, 1),
+            "frac_of_peak": round(gbs / peak, 4), "threads": sim.threads,
+            "tile_cells": sim.tile_cells}
+        del flows, colls, sim
+        torch.cuda.empty_cache()
+    out["config4_batched"] = c4
+
+    nn = 512
+    ulu = 0.05 / math.sqrt(3)
+    x = torch.arange(nn, dtype=torch.float64) * 2 * math.pi / nn
+    XX, YY = torch.meshgrid(x, x, indexing="ij")
+    u0 = torch.stack([torch.cos(XX) * torch.sin(YY), -torch.sin(XX) * torch.cos(YY)]) * ulu
+    u0 = u0 + 1e-3 * torch.randn(u0.shape, generator=torch.Generator().manual_seed(0),
+                                 dtype=torch.float64)
+    target = ulu * torch.randn(u0.shape, generator=torch.Generator().manual_seed(1),
+                               dtype=torch.float64)
+    tau = 3 * ((nn / (2 * math.pi)) * ulu / 1000) + 0.5
+    u0 = u0.float().to(device)
+    target = target.float().to(device)
+    carrier = lt.TaylorGreenVortex(lt.Context(device, torch.float32), nn, 1000, 0.05, lt.D2Q9)
+    rho0 = torch.ones([1, nn, nn], dtype=torch.float32, device=device)
+    times = []
+    for _ in range(3):
+        u = u0.clone().requires_grad_(True)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        f0 = lt.QuadraticEquilibrium()(carrier, rho0, u)
+        fT = lt.rollout(f0, carrier.stencil, tau, 200, checkpoint_every=20)
+        _, uT = lt.moments_torch(fT, carrier.stencil)
+        loss = torch.mean((uT - target) ** 2)
+        torch.cuda.synchronize(device)
+        t1 = time.perf_counter()
+        loss.backward()
+        torch.cuda.synchronize(device)
+        times.append((t1 - t0, time.perf_counter() - t1))
+    fwd, bwd = min(t[0] for t in times), min(t[1] for t in times)
+    out["config5_adjoint"] = {
+        "workload": "D2Q9 BGK 512^2 float32, 200 steps, checkpoint every 20",
+        "forward_ms": round(fwd * 1e3, 2), "backward_ms": round(bwd * 1e3, 2),
+        "forward_mlups": round(200 * nn * nn / fwd / 1e6, 1),
+        "note": "host wall clock around synchronised calls, best of 3"}
+    del carrier
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import lettuce_gb300 as lt
@@ -347,6 +466,10 @@ def run_ours(args, world, rank, local):
     if not args.no_accuracy:
         acc = accuracy_fp16(lt, torch, device, steps=args.accuracy_steps)
 
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = measure_configs(lt, torch, device, peak)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
@@ -383,6 +506,7 @@ def run_ours(args, world, rank, local):
                 "call": f"flow.f = pinned host field; simulation({args.steps}); field back to "
                         "pinned host"},
         "cpu_baseline": cpu,
+        "configs": configs,
         "clocks": clocks,
         "gpu_launches": args.steps,
     }
@@ -399,6 +523,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the KBC obstacle, batched and adjoint configurations")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--grid", type=int, default=256,
                     help="cube side (profiling a smaller case; the benchmark is 256)")

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define LGB_ABI_VERSION 1
+#define LGB_ABI_VERSION 2
 #define LGB_MAX_SUBSTEPS 8
 
 /* stencils (lettuce/ext/_stencil/d1q3.py, d2q9.py, d3q15.py, d3q19.py, d3q27.py) */
@@ -31,8 +31,24 @@ enum { LGB_D1Q3 = 1, LGB_D2Q9 = 2, LGB_D3Q15 = 3, LGB_D3Q19 = 4, LGB_D3Q27 = 5 }
  * for LGB_F64. */
 enum { LGB_F64 = 0, LGB_F32 = 1, LGB_F16_SHIFTED = 2, LGB_BF16_SHIFTED = 3 };
 
-/* collision operators (lettuce/ext/_collision/) */
-enum { LGB_NO_COLLISION = 0, LGB_BGK = 1, LGB_TRT = 2, LGB_KBC = 3 };
+/* collision operators (lettuce/ext/_collision/): no_collision.py,
+ * bgk_collision.py, trt_collision.py, kbc_collision.py,
+ * regularized_collision.py, smagorinsky_collision.py */
+enum {
+    LGB_NO_COLLISION = 0, LGB_BGK = 1, LGB_TRT = 2, LGB_KBC = 3, LGB_REGULARIZED = 4,
+    LGB_SMAGORINSKY = 5, LGB_MRT = 6
+};
+
+/* equilibrium moments of the MRT collision (lettuce/ext/_collision/mrt_collision.py
+ * with the transforms of lettuce/util/moments.py): GENERIC = M feq(rho, u)
+ * (Transform.equilibrium), DELLAR / LALLEMAND = the D2Q9 bases' formulas,
+ * HERMITE = the D3Q27 Hermite basis' formulas */
+enum { LGB_MRT_EQ_GENERIC = 0, LGB_MRT_EQ_DELLAR = 1, LGB_MRT_EQ_LALLEMAND = 2,
+       LGB_MRT_EQ_HERMITE = 3 };
+
+/* body forces of BGK and Smagorinsky (lettuce/ext/_force/guo.py,
+ * shan_chen.py): a constant acceleration in lattice units */
+enum { LGB_FORCE_NONE = 0, LGB_FORCE_GUO = 1, LGB_FORCE_SHAN_CHEN = 2 };
 
 /* substeps of the masked collide, in lettuce's order pre-boundaries,
  * collision, post-boundaries (lettuce/_simulation.py:258-305) */
@@ -94,7 +110,7 @@ typedef struct {
     int32_t collision;
     int32_t pattern;
     int32_t res[3];          /* lettuce resolution; unused trailing dims = 1 */
-    double tau;              /* BGK tau, TRT tau_plus, KBC tau */
+    double tau;              /* BGK, KBC, regularized and Smagorinsky tau; TRT tau_plus */
     double tau_minus;        /* TRT */
     const void *f_in;        /* [Q][N] in `storage` */
     void *f_out;             /* [Q][N]; == f_in for LGB_LOCAL / AA patterns */
@@ -105,7 +121,17 @@ typedef struct {
     lgb_substep sub[LGB_MAX_SUBSTEPS];
     uint32_t *status;        /* optional device word; bit 0 set on a non-finite density */
     int32_t options;         /* LGB_OPT_* bits */
-    int32_t reserved;
+    int32_t force;           /* LGB_FORCE_*; BGK and Smagorinsky only */
+    double force_tau;        /* the force's tau (Guo: source factor 1 - 1/(2 tau);
+                                Shan-Chen: velocity shift tau a / rho) */
+    double accel[3];         /* acceleration, lattice units, lettuce dimension order */
+    double smagorinsky_constant; /* LGB_SMAGORINSKY: C (lettuce default 0.17) */
+    int32_t mrt_equilibrium;  /* LGB_MRT: LGB_MRT_EQ_* */
+    int32_t reserved2;
+    const double *mrt_tables; /* LGB_MRT, HOST memory read during the call: the
+                                 moment matrix M [Q][Q] (row-major), its inverse
+                                 [Q][Q] and the Q relaxation times s_i
+                                 (m_i <- m_i - (m_i - meq_i) / s_i) */
 } lgb_step_desc;
 
 /* options: run the one-cell-per-thread kernel even where the two-cell

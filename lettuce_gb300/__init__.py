@@ -13,14 +13,17 @@ from ._stencil import D1Q3, D2Q9, D3Q15, D3Q19, D3Q27, Stencil, TorchStencil
 from ._unit import UnitConversion
 from ._flow import (Boundary, Equilibrium, Flow, QuadraticEquilibrium,
                     initialize_f_neq, torch_gradient)
-from ._collision import BGKCollision, Collision, KBCCollision, NoCollision, TRTCollision
+from ._collision import (BGKCollision, Collision, KBCCollision, MRTCollision, NoCollision,
+                         RegularizedCollision, SmagorinskyCollision, TRTCollision)
+from ._moments import D1Q3Transform, D2Q9Dellar, D2Q9Lallemand, D3Q27Hermite, Transform
+from ._force import Force, Guo, ShanChen
 from ._boundary import (AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU,
                         EquilibriumOutletP, PartiallySaturatedBC)
 from ._simulation import BreakableSimulation, Reporter, Simulation, StreamingStrategy
 from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporterBase,
                         HighMaReporter, IncompressibleKineticEnergy, Mass,
                         MaximumVelocity, NaNReporter, Observable, ObservableReporter)
-from ._flows import ExtFlow, Obstacle, TaylorGreenVortex
+from ._flows import ExtFlow, Obstacle, PoiseuilleFlow2D, TaylorGreenVortex
 from ._native import NativeBoundary, NativeCollision, NativeEquilibrium
 from ._batched import BatchedSimulation, batched_taylor_green
 from ._adjoint import moments_torch, rollout
@@ -41,5 +44,7 @@ __all__ = [
     "NaNReporter", "HighMaReporter", "ExtFlow", "TaylorGreenVortex", "Obstacle",
     "NativeBoundary", "NativeCollision", "NativeEquilibrium", "BatchedSimulation",
     "batched_taylor_green", "rollout", "moments_torch", "Slab", "SlabSimulation",
-    "exchange", "exchange_local",
+    "exchange", "exchange_local", "RegularizedCollision", "SmagorinskyCollision", "Force",
+    "Guo", "ShanChen", "PoiseuilleFlow2D", "MRTCollision", "Transform", "D1Q3Transform",
+    "D2Q9Dellar", "D2Q9Lallemand", "D3Q27Hermite",
 ]

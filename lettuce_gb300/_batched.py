@@ -26,6 +26,7 @@ __all__ = ["BatchedSimulation", "plan_tiles", "batched_taylor_green"]
 
 DOMAIN_DTYPE = np.dtype([("offset", "<i8"), ("res", "<i4", (3,)), ("reserved", "<i4"),
                          ("tau", "<f8"), ("tau_minus", "<f8")])
+POOL_ALIGN = 128  # elements
 TILE_DTYPE = np.dtype([("domain", "<i4"), ("row_begin", "<i4"), ("row_end", "<i4"),
                        ("reserved", "<i4")])
 
@@ -95,8 +96,12 @@ class BatchedSimulation:
         q = self.stencil.q
         dom = np.zeros(len(flows), dtype=DOMAIN_DTYPE)
         off = 0
+        cells = 0
         for b, (fl, c) in enumerate(zip(flows, collisions)):
             res = list(fl.resolution) + [1] * (3 - len(fl.resolution))
+            # every domain starts on a 128-element boundary of the pool, so the
+            # two-cell kernel of the 16-bit formats reads whole aligned words
+            off = -(-off // POOL_ALIGN) * POOL_ALIGN
             dom[b]["offset"] = off
             dom[b]["res"] = res
             if isinstance(c, TRTCollision):
@@ -106,9 +111,10 @@ class BatchedSimulation:
             else:
                 dom[b]["tau"], dom[b]["tau_minus"] = 1.0, 1.0
             off += q * int(np.prod(fl.resolution))
+            cells += int(np.prod(fl.resolution))
         self.domains = dom
         self.pool_elements = off
-        self.n_cells = off // q
+        self.n_cells = cells
         dev = self.context.device
         sdt = self.context.storage_dtype
         self._pools = [torch.empty(off, dtype=sdt, device=dev),

@@ -8,12 +8,14 @@ from __future__ import annotations
 from abc import ABC, abstractmethod
 from typing import Optional
 
+import numpy as np
 import torch
 
 from . import _lib
 from ._native import NativeCollision
 
-__all__ = ["Collision", "BGKCollision", "TRTCollision", "KBCCollision", "NoCollision"]
+__all__ = ["Collision", "BGKCollision", "TRTCollision", "KBCCollision", "NoCollision",
+           "RegularizedCollision", "SmagorinskyCollision", "MRTCollision"]
 
 
 class Collision(ABC):
@@ -54,11 +56,11 @@ class BGKCollision(Collision):
         return self.__class__.__name__
 
     def native_available(self) -> bool:
-        # forcing terms (Guo, Shan-Chen) are not part of the fused kernels
-        return self.force is None
+        return self.force is None or self.force.native_available()
 
     def native_generator(self, index: int) -> NativeCollision:
-        return NativeCollision(_lib.BGK, index, tau=float(self.tau))
+        force = self.force.native_generator() if self.force is not None else None
+        return NativeCollision(_lib.BGK, index, tau=float(self.tau), force=force)
 
 
 class TRTCollision(Collision):
@@ -110,6 +112,95 @@ class KBCCollision(Collision):
         if self.tau is None:
             raise RuntimeError("KBCCollision needs a flow (Simulation binds it) before use")
         return NativeCollision(_lib.KBC, index, tau=float(self.tau))
+
+
+class RegularizedCollision(Collision):
+    """regularized BGK (Latt & Chopard 2006,
+    lettuce/ext/_collision/regularized_collision.py:8-47): the non-equilibrium
+    part is replaced by its projection on the second moments,
+    f = feq + (1 - 1/tau) w_q Q_q : Pi_neq / (2 cs^4). Like lettuce, it
+    relaxes with the flow's ``units.relaxation_parameter_lu`` (the
+    constructor argument is overwritten when bound to a flow)."""
+
+    def __init__(self, tau: float = None):
+        self.tau = tau
+
+    def bind(self, flow):
+        self.tau = flow.units.relaxation_parameter_lu
+
+    def __call__(self, flow) -> torch.Tensor:
+        return self._apply_standalone(flow)
+
+    def native_available(self) -> bool:
+        return True
+
+    def native_generator(self, index: int) -> NativeCollision:
+        if self.tau is None:
+            raise RuntimeError("RegularizedCollision needs a flow (Simulation binds it) before use")
+        return NativeCollision(_lib.REGULARIZED, index, tau=float(self.tau))
+
+
+class SmagorinskyCollision(Collision):
+    """Smagorinsky large-eddy BGK
+    (lettuce/ext/_collision/smagorinsky_collision.py:8-41): per cell,
+    tau_eff from two fixed-point iterations of
+    nu_eff = (tau - 1/2)/3 + C^2 S:S with S = Pi_neq / (2 rho cs^2 tau_eff),
+    optionally with a body force"""
+
+    def __init__(self, tau, smagorinsky_constant=0.17, force: Optional[object] = None):
+        self.force = force
+        self.tau = tau
+        self.iterations = 2
+        self.tau_eff = tau
+        self.constant = smagorinsky_constant
+
+    def __call__(self, flow) -> torch.Tensor:
+        return self._apply_standalone(flow)
+
+    def native_available(self) -> bool:
+        return self.force is None or self.force.native_available()
+
+    def native_generator(self, index: int) -> NativeCollision:
+        force = self.force.native_generator() if self.force is not None else None
+        return NativeCollision(_lib.SMAGORINSKY, index, tau=float(self.tau), force=force,
+                               smagorinsky_constant=float(self.constant))
+
+
+class MRTCollision(Collision):
+    """multiple-relaxation-time collision
+    (lettuce/ext/_collision/mrt_collision.py:8-30): m = M f,
+    m <- m - (m - meq) / s, f = M^-1 m, with the moment basis and equilibrium
+    of ``transform`` (``lettuce_gb300._moments``) and one relaxation time per
+    moment"""
+
+    def __init__(self, transform, relaxation_parameters: list, context):
+        self.transform = transform
+        self.relaxation_parameters = context.convert_to_tensor(relaxation_parameters)
+
+    def __call__(self, flow) -> torch.Tensor:
+        return self._apply_standalone(flow)
+
+    def _equilibrium_kind(self):
+        """the kernel's equilibrium for the transform: that of the class of
+        this package defining the transform's ``equilibrium``, or None"""
+        from . import _moments
+        owner = next((k for k in type(self.transform).__mro__ if "equilibrium" in k.__dict__),
+                     None)
+        if owner is None or owner.__module__ != _moments.__name__:
+            return None
+        return owner.__dict__.get("equilibrium_kind", _lib.MRT_EQ_GENERIC)
+
+    def native_available(self) -> bool:
+        return self._equilibrium_kind() is not None
+
+    def native_generator(self, index: int) -> NativeCollision:
+        kind = self._equilibrium_kind()
+        if kind is None:
+            raise NotImplementedError(f"no kernel for the transform {type(self.transform).__name__}")
+        s = self.relaxation_parameters.detach().to("cpu", torch.float64).numpy().reshape(-1)
+        tables = np.concatenate([self.transform.matrix_np.reshape(-1),
+                                 self.transform.inverse_np.reshape(-1), s])
+        return NativeCollision(_lib.MRT, index, mrt_equilibrium=kind, mrt_tables=tables)
 
 
 class NoCollision(Collision):

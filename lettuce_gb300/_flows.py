@@ -1,5 +1,6 @@
-"""Problem set-ups: lettuce's ExtFlow, TaylorGreenVortex and Obstacle
-(lettuce/ext/_flows/_ext_flow.py, taylorgreen.py, obstacle.py) with the same
+"""Problem set-ups: lettuce's ExtFlow, TaylorGreenVortex, Obstacle and
+PoiseuilleFlow2D (lettuce/ext/_flows/_ext_flow.py, taylorgreen.py,
+obstacle.py, poiseuille.py) with the same
 constructors, unit conventions, initial fields and boundary lists."""
 from __future__ import annotations
 
@@ -15,7 +16,7 @@ from ._flow import Flow, QuadraticEquilibrium
 from ._stencil import D1Q3, D2Q9, D3Q19
 from ._unit import UnitConversion
 
-__all__ = ["ExtFlow", "TaylorGreenVortex", "Obstacle"]
+__all__ = ["ExtFlow", "TaylorGreenVortex", "Obstacle", "PoiseuilleFlow2D"]
 
 
 class ExtFlow(Flow, ABC):
@@ -172,3 +173,62 @@ class Obstacle(ExtFlow):
 
     def _unit_vector(self, i=0):
         return torch.eye(self.stencil.d)[i]
+
+
+class PoiseuilleFlow2D(ExtFlow):
+    """plane Poiseuille channel driven by a body force a = (0.001, 0)
+    (physical units) between bounce-back walls at y = 0 and y = 1,
+    periodic in x (lettuce/ext/_flows/poiseuille.py:16-95); starts at rest by
+    default"""
+
+    def __init__(self, context, resolution: Union[int, List[int]], reynolds_number,
+                 mach_number, stencil=None, equilibrium=None, initialize_with_zeros=True):
+        self.stencil = D2Q9() if stencil is None else (stencil() if callable(stencil) else stencil)
+        self.initialize_with_zeros = initialize_with_zeros
+        ExtFlow.__init__(self, context, resolution, reynolds_number, mach_number,
+                         self.stencil, equilibrium)
+
+    def analytic_solution(self, t=0):
+        half_lattice_spacing = 0.5 / self.resolution[0]
+        x, y = self.grid
+        nu = self.units.viscosity_pu
+        rho = 1
+        ux = (self.acceleration[0] / (2 * rho * nu)
+              * ((y - half_lattice_spacing) * (1 - half_lattice_spacing - y)))
+        uy = self.context.zero_tensor(self.resolution)
+        u = torch.stack([ux, uy], dim=0)
+        p = y * 0 + self.units.convert_density_lu_to_pressure_pu(rho)
+        return p, u
+
+    def initial_pu(self):
+        if self.initialize_with_zeros:
+            zeros = self.context.zero_tensor(self.resolution)
+            return zeros[None, ...], torch.stack(2 * [zeros], dim=0)
+        return self.analytic_solution()
+
+    def make_units(self, reynolds_number, mach_number, resolution) -> UnitConversion:
+        return UnitConversion(reynolds_number=reynolds_number, mach_number=mach_number,
+                              characteristic_length_lu=resolution[0] - 1,
+                              characteristic_length_pu=1, characteristic_velocity_pu=1)
+
+    def make_resolution(self, resolution, stencil=None) -> List[int]:
+        if isinstance(resolution, list):
+            assert len(resolution) == self.stencil.d
+            return list(resolution)
+        return [resolution] * self.stencil.d
+
+    @property
+    def grid(self):
+        xyz = tuple(torch.linspace(0, 1, steps=n, device=self.context.device,
+                                   dtype=self.context.dtype) for n in self.resolution)
+        return torch.meshgrid(*xyz, indexing="ij")
+
+    @property
+    def post_boundaries(self):
+        mask = self.context.zero_tensor(self.resolution, dtype=bool)
+        mask[:, [0, -1]] = True
+        return [BounceBackBoundary(mask=mask)]
+
+    @property
+    def acceleration(self):
+        return self.context.convert_to_tensor([0.001, 0])

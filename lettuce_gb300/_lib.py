@@ -12,14 +12,16 @@ import threading
 
 from . import build as _build
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_SUBSTEPS = 8
 REDUCE_FIELDS = 5
 
 # enums of include/lettuce_gb300.h
 D1Q3, D2Q9, D3Q15, D3Q19, D3Q27 = 1, 2, 3, 4, 5
 F64, F32, F16_SHIFTED, BF16_SHIFTED = 0, 1, 2, 3
-NO_COLLISION, BGK, TRT, KBC = 0, 1, 2, 3
+NO_COLLISION, BGK, TRT, KBC, REGULARIZED, SMAGORINSKY, MRT = 0, 1, 2, 3, 4, 5, 6
+MRT_EQ_GENERIC, MRT_EQ_DELLAR, MRT_EQ_LALLEMAND, MRT_EQ_HERMITE = 0, 1, 2, 3
+FORCE_NONE, FORCE_GUO, FORCE_SHAN_CHEN = 0, 1, 2
 SUB_COLLISION, SUB_BOUNCE_BACK, SUB_EQUILIBRIUM_PU, SUB_ANTI_BOUNCE_BACK, SUB_NONE = 0, 1, 2, 3, 4
 SUB_EQUILIBRIUM_OUTLET_P, SUB_PARTIALLY_SATURATED = 5, 6
 PULL, PUSH, LOCAL, AA_EVEN, AA_ODD, STREAM_ONLY, AA_UNPACK = 0, 1, 2, 3, 4, 5, 6
@@ -62,7 +64,13 @@ class StepDesc(ctypes.Structure):
                 ("sub", Substep * MAX_SUBSTEPS),
                 ("status", ctypes.c_void_p),
                 ("options", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("force", ctypes.c_int32),
+                ("force_tau", ctypes.c_double),
+                ("accel", ctypes.c_double * 3),
+                ("smagorinsky_constant", ctypes.c_double),
+                ("mrt_equilibrium", ctypes.c_int32),
+                ("reserved2", ctypes.c_int32),
+                ("mrt_tables", ctypes.c_void_p)]
 
 
 class LibraryError(RuntimeError):

@@ -16,7 +16,7 @@ import torch
 from . import _lib
 
 __all__ = ["NativeEquilibrium", "NativeQuadraticEquilibrium", "NativeCollision",
-           "NativeBoundary"]
+           "NativeBoundary", "NativeForce"]
 
 
 @dataclass
@@ -29,11 +29,22 @@ def NativeQuadraticEquilibrium() -> NativeEquilibrium:
 
 
 @dataclass
+class NativeForce:
+    kind: int                  # _lib.FORCE_GUO / FORCE_SHAN_CHEN
+    tau: float
+    acceleration: tuple        # lattice units, one entry per dimension
+
+
+@dataclass
 class NativeCollision:
-    kind: int                  # _lib.NO_COLLISION / BGK / TRT / KBC
+    kind: int                  # _lib.NO_COLLISION / BGK / TRT / KBC / REGULARIZED / SMAGORINSKY
     index: int
     tau: float = 1.0
     tau_minus: float = 1.0
+    force: Optional[NativeForce] = None
+    smagorinsky_constant: float = 0.0
+    mrt_equilibrium: int = 0
+    mrt_tables: Optional[object] = None  # float64 numpy [M, M^-1, relaxation times]
 
 
 @dataclass

@@ -23,6 +23,7 @@ from functools import lru_cache
 from timeit import default_timer as timer
 from typing import List, Optional, Sequence
 
+import numpy as np
 import torch
 
 from . import _device, _lib
@@ -91,7 +92,19 @@ def _desc_for(flow, natives, flags, nsb, collision_index, res=None):
     d.collision = coll.kind
     d.tau = coll.tau
     d.tau_minus = coll.tau_minus
+    d.smagorinsky_constant = coll.smagorinsky_constant
     keep = []
+    if coll.force is not None:
+        d.force = coll.force.kind
+        d.force_tau = coll.force.tau
+        for k, a in enumerate(coll.force.acceleration):
+            d.accel[k] = float(a)
+    if coll.mrt_tables is not None:
+        # host memory read by lgb_step at each call: kept alive with the desc
+        tables = np.ascontiguousarray(coll.mrt_tables, dtype=np.float64)
+        keep.append(tables)
+        d.mrt_equilibrium = coll.mrt_equilibrium
+        d.mrt_tables = tables.ctypes.data
     if flags is not None:
         if len(natives) > _lib.MAX_SUBSTEPS:
             raise ValueError(f"at most {_lib.MAX_SUBSTEPS} substeps (boundaries + collision)")

@@ -49,6 +49,9 @@ def _units():
         for s in range(N_STORAGES):
             units.append((f"step_{st}_s{s}.o", f"lgb_step_{st}.cu",
                           [f"-DLGB_STORAGE_ID={s}"]))
+            # forced BGK, regularized and Smagorinsky: their own objects
+            units.append((f"stepx_{st}_s{s}.o", f"lgb_step_{st}.cu",
+                          [f"-DLGB_STORAGE_ID={s}", "-DLGB_EXT_COLLISIONS=1"]))
     for src in sorted(os.listdir(CSRC)):
         if src.endswith(".cu") and not src.startswith("lgb_step_"):
             units.append((src[:-3] + ".o", src, []))

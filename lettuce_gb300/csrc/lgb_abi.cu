@@ -88,6 +88,18 @@ cudaError_t dispatch_step(int stencil, int storage, int coll, int pat, bool mask
     case 3: return lgb::name##_s3(coll, pat, masked, p, s);                 \
     }                                                                       \
     return cudaErrorInvalidValue;
+    const bool ext = coll == lgb::LGB_BGK_FORCED || coll == LGB_REGULARIZED ||
+                     coll == LGB_SMAGORINSKY || coll == LGB_MRT;
+    if (ext) {
+        switch (stencil) {
+        case LGB_D1Q3: LGB_STORAGE_SWITCH(stepx_d1q3)
+        case LGB_D2Q9: LGB_STORAGE_SWITCH(stepx_d2q9)
+        case LGB_D3Q15: LGB_STORAGE_SWITCH(stepx_d3q15)
+        case LGB_D3Q19: LGB_STORAGE_SWITCH(stepx_d3q19)
+        case LGB_D3Q27: LGB_STORAGE_SWITCH(stepx_d3q27)
+        }
+        return cudaErrorInvalidValue;
+    }
     switch (stencil) {
     case LGB_D1Q3: LGB_STORAGE_SWITCH(step_d1q3)
     case LGB_D2Q9: LGB_STORAGE_SWITCH(step_d2q9)
@@ -390,8 +402,30 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     Grid g;
     if (make_grid(d->stencil, d->res, &g)) return -1;
     if (!valid_storage(d->storage)) return fail("lgb_step: unknown storage id %d", d->storage);
-    if (d->collision < LGB_NO_COLLISION || d->collision > LGB_KBC)
+    if (d->collision < LGB_NO_COLLISION || d->collision > LGB_MRT)
         return fail("lgb_step: unknown collision id %d", d->collision);
+    if (d->collision == LGB_MRT) {
+        if (!d->mrt_tables) return fail("lgb_step: the MRT collision needs its tables");
+        if (d->mrt_equilibrium < LGB_MRT_EQ_GENERIC || d->mrt_equilibrium > LGB_MRT_EQ_HERMITE)
+            return fail("lgb_step: unknown MRT equilibrium %d", d->mrt_equilibrium);
+        if ((d->mrt_equilibrium == LGB_MRT_EQ_DELLAR || d->mrt_equilibrium == LGB_MRT_EQ_LALLEMAND) &&
+            d->stencil != LGB_D2Q9)
+            return fail("lgb_step: the Dellar and Lallemand moment bases are D2Q9 bases");
+        if (d->mrt_equilibrium == LGB_MRT_EQ_HERMITE && d->stencil != LGB_D3Q27)
+            return fail("lgb_step: the Hermite moment basis is a D3Q27 basis");
+        const int Q = g.q;
+        for (int i = 0; i < Q; ++i) {
+            const double s = d->mrt_tables[2 * Q * Q + i];
+            if (!(s != 0.0) || !std::isfinite(s))
+                return fail("lgb_step: MRT relaxation time %d is %g", i, s);
+        }
+    }
+    if (d->force < LGB_FORCE_NONE || d->force > LGB_FORCE_SHAN_CHEN)
+        return fail("lgb_step: unknown force id %d", d->force);
+    if (d->force != LGB_FORCE_NONE && d->collision != LGB_BGK && d->collision != LGB_SMAGORINSKY)
+        return fail("lgb_step: a body force needs the BGK or Smagorinsky collision");
+    if (d->force != LGB_FORCE_NONE && !(d->force_tau > 0.0))
+        return fail("lgb_step: the force's tau must be positive (got %g)", d->force_tau);
     if (d->collision == LGB_KBC && !(d->stencil == LGB_D2Q9 || d->stencil == LGB_D3Q27))
         return fail("lgb_step: KBC collision is only defined for D2Q9 and D3Q27");
     if (d->pattern < LGB_PULL || d->pattern > LGB_AA_UNPACK)
@@ -400,7 +434,7 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     const bool in_place_ok = d->pattern == LGB_LOCAL || d->pattern == LGB_AA_EVEN || d->pattern == LGB_AA_ODD;
     if (!in_place_ok && d->f_in == d->f_out)
         return fail("lgb_step: pattern %d needs distinct input and output fields", d->pattern);
-    if (d->collision != LGB_NO_COLLISION && !(d->tau > 0.0))
+    if (d->collision != LGB_NO_COLLISION && d->collision != LGB_MRT && !(d->tau > 0.0))
         return fail("lgb_step: relaxation time must be positive (got %g)", d->tau);
     if (d->collision == LGB_TRT && !(d->tau_minus > 0.0))
         return fail("lgb_step: TRT tau_minus must be positive (got %g)", d->tau_minus);
@@ -416,6 +450,15 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     p.cp.inv_2tp = 1.0 / (2.0 * d->tau);
     p.cp.inv_2tm = d->collision == LGB_TRT ? 1.0 / (2.0 * d->tau_minus) : 0.0;
     p.cp.beta = 1.0 / (2.0 * d->tau);
+    p.cp.tau = d->tau;
+    p.cp.smag_c2 = d->smagorinsky_constant * d->smagorinsky_constant;
+    p.mrt_host = d->mrt_tables;
+    p.mrt_eq = d->mrt_equilibrium;
+    if (d->force != LGB_FORCE_NONE) {
+        for (int i = 0; i < 3; ++i) p.cp.accel[i] = i < g.d ? d->accel[i] : 0.0;
+        p.cp.ueq_scale = d->force == LGB_FORCE_GUO ? 0.5 : d->force_tau;
+        p.cp.src_scale = d->force == LGB_FORCE_GUO ? 1.0 - 1.0 / (2.0 * d->force_tau) : 0.0;
+    }
     p.status = d->status;
     p.abb_k = -1;
     const bool masked = d->flags != nullptr;
@@ -480,12 +523,15 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (p.abb_k >= 0 && d->f_in == d->f_out)
         return fail("lgb_step: the anti-bounce-back outlet reads its neighbour plane and "
                     "needs distinct input and output fields");
+    // the kernel variant: BGK with a force is its own collision kind
+    const int coll = d->collision == LGB_BGK && d->force != LGB_FORCE_NONE ? lgb::LGB_BGK_FORCED
+                                                                            : d->collision;
     const bool vec2 = !(d->options & LGB_OPT_ONE_CELL) &&
-                      use_vec2(d->storage, d->collision, d->pattern, masked, g.Z);
+                      use_vec2(d->storage, coll, d->pattern, masked, g.Z);
     cudaError_t e = vec2
-                        ? dispatch_step_vec2(d->stencil, d->storage, d->collision, d->pattern, p,
+                        ? dispatch_step_vec2(d->stencil, d->storage, coll, d->pattern, p,
                                              static_cast<cudaStream_t>(stream))
-                        : dispatch_step(d->stencil, d->storage, d->collision, d->pattern, masked,
+                        : dispatch_step(d->stencil, d->storage, coll, d->pattern, masked,
                                         p, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "lgb_step: launch failed");
     return 0;

@@ -4,11 +4,15 @@
 // host cuts every domain into tiles of whole rows (lgb_batch_plan) and the
 // kernel's resident blocks walk the tile table with a grid stride, one cell
 // per thread, pulling from the periodic neighbours inside the tile's domain.
-// The per-domain relaxation times come from the domain table.
+// The per-domain relaxation times come from the domain table. Domains of the
+// 16-bit formats with an even row length (and a word-aligned offset) run the
+// two-cell step (one 32-bit word per population pair, lgb_step_vec.cuh),
+// bit-identical to the one-cell step.
 #pragma once
 
 #include "lgb_shifted.cuh"
 #include "lgb_step.cuh"
+#include "lgb_step_vec.cuh"
 
 namespace lgb {
 
@@ -70,6 +74,19 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
         T *fout = pool_out + dom.offset;
         const uint32_t first = (uint32_t)tile.row_begin * g.Z;
         const uint32_t last = (uint32_t)tile.row_end * g.Z;
+        if constexpr (HSPACE) {
+            if ((g.Z & 1u) == 0 && (dom.offset & 1) == 0) {
+                g.f_in = fin;
+                g.f_out = fout;
+                g.divZ = FastDiv::make_device(g.Z >> 1);
+                g.divY = divY;
+                g.cp = cp;
+                g.status = p.status;
+                for (uint32_t t2 = (first >> 1) + threadIdx.x; t2 < (last >> 1); t2 += blockDim.x)
+                    step_pair<SID, ST, COLL, LGB_PULL>(g, t2);
+                continue;
+            }
+        }
         for (uint32_t n = first + threadIdx.x; n < last; n += blockDim.x) {
             const uint32_t row = divZ.div(n);
             const uint32_t z = n - row * g.Z;

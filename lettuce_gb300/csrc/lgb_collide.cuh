@@ -8,6 +8,13 @@
 //   BGK          lettuce/ext/_collision/bgk_collision.py:17-22
 //   TRT          lettuce/ext/_collision/trt_collision.py:16-27
 //   KBC          lettuce/ext/_collision/kbc_collision.py:22-160
+//   forced BGK   lettuce/ext/_collision/bgk_collision.py:17-22 with
+//                lettuce/ext/_force/guo.py:17-36, shan_chen.py:13-24
+//   regularized  lettuce/ext/_collision/regularized_collision.py:17-47
+//   Smagorinsky  lettuce/ext/_collision/smagorinsky_collision.py:22-41
+//   MRT          lettuce/ext/_collision/mrt_collision.py:23-30 with the
+//                equilibria of lettuce/util/moments.py:92-104, 180-204,
+//                240-274, 511-545
 #pragma once
 
 #include "lgb_stencil.cuh"
@@ -66,11 +73,23 @@ LGB_HD void set_equilibrium(R (&f)[S::Q], R rho, const R (&u)[3]) {
     for (int q = 0; q < S::Q; ++q) f[q] = feq_q<S>(q, rho, u, uu);
 }
 
+// collision kinds beyond the ABI's: BGK with a body force (the ABI's BGK
+// with a force descriptor) is its own kernel variant
+constexpr int LGB_BGK_FORCED = 16;
+
 struct CollideParams {
     double omega;        // 1 / tau (BGK)
     double inv_2tp;      // 1 / (2 tau_plus) (TRT)
     double inv_2tm;      // 1 / (2 tau_minus) (TRT)
     double beta;         // 1 / (2 tau) (KBC)
+    // body force (forced BGK, Smagorinsky): constant acceleration a (lattice
+    // units), equilibrium velocity u = j / rho + ueq_scale a / rho, source
+    // term src_scale w_q [(e_q - u) / cs^2 + (e_q . u) e_q / cs^4] . a
+    double accel[3];
+    double ueq_scale;    // Guo: 1/2; Shan-Chen: the force's tau; none: 0
+    double src_scale;    // Guo: 1 - 1 / (2 tau_force); otherwise 0
+    double tau;          // Smagorinsky: the molecular relaxation time
+    double smag_c2;      // Smagorinsky constant squared
 };
 
 template <class S, class R>
@@ -203,16 +222,18 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
             return -ds_val[3];
         }
     };
-    R dh[S::Q];
+    // delta_h is formed twice (for the entropy sums, then for the update)
+    // rather than kept in Q more registers
+    auto delta_h = [&](int q) -> R { return f[q] - feq_q<S>(q, rho, u, uu) - ds(q); };
     R sum_s = R(0), sum_h = R(0);
 #pragma unroll
     for (int q = 0; q < S::Q; ++q) {
         const R feq = feq_q<S>(q, rho, u, uu);
         const R d_s = ds(q);
-        dh[q] = f[q] - feq - d_s;
+        const R dh = f[q] - feq - d_s;
         const R ifeq = kbc_rcp(feq);
-        sum_s += d_s * dh[q] * ifeq;
-        sum_h += dh[q] * dh[q] * ifeq;
+        sum_s += d_s * dh * ifeq;
+        sum_h += dh * dh * ifeq;
     }
     const R beta = R(cp.beta);
     const R ib = R(1) / beta;
@@ -221,18 +242,244 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     if (!(gamma >= R(1e-15))) gamma = R(2);
     const R b2 = R(2) * beta, bg = beta * gamma;
 #pragma unroll
-    for (int q = 0; q < S::Q; ++q) f[q] = f[q] - b2 * ds(q) - bg * dh[q];
+    for (int q = 0; q < S::Q; ++q) {
+        const R dh = delta_h(q);
+        f[q] = f[q] - b2 * ds(q) - bg * dh;
+    }
     rho_out = rho;
 }
 
-template <int COLL, class S, class R>
-LGB_HD void collide(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+// j / rho + ueq_scale a / rho (forced BGK and Smagorinsky,
+// bgk_collision.py:18-19 with Force.u_eq)
+template <class S, class R>
+LGB_HD void forced_velocity(const R (&f)[S::Q], const CollideParams &cp, R &rho, R (&u)[3]) {
+    cell_moments<S>(f, rho, u);
+    if (cp.ueq_scale != 0.0) {
+        const R s = R(cp.ueq_scale) / rho;
+#pragma unroll
+        for (int d = 0; d < S::D; ++d) u[d] += s * R(cp.accel[d]);
+    }
+}
+
+// Guo's source term of population q (guo.py:17-28), zero when src_scale is 0
+template <class S, class R>
+LGB_HD R guo_source(int q, const CollideParams &cp, const R (&u)[3]) {
+    R eu = R(0), ea = R(0), ua = R(0);
+#pragma unroll
+    for (int d = 0; d < S::D; ++d) {
+        const int c = S::e(q, d);
+        const R a = R(cp.accel[d]);
+        if (c == 1) { eu += u[d]; ea += a; }
+        else if (c == -1) { eu -= u[d]; ea -= a; }
+        ua += u[d] * a;
+    }
+    // ((e - u) / cs^2 + (e.u) e / cs^4) . a with cs^2 = 1/3
+    const R t = R(3) * (ea - ua) + R(9) * eu * ea;
+    return R(cp.src_scale) * R(S::w(q)) * t;
+}
+
+template <class S, class R>
+LGB_HD void collide_bgk_forced(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+    R rho, u[3];
+    forced_velocity<S>(f, cp, rho, u);
+    const R uu = dot_uu<S>(u);
+    const R om = R(cp.omega);
+    const bool src = cp.src_scale != 0.0;
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        R v = f[q] - om * (f[q] - feq_q<S>(q, rho, u, uu));
+        if (src) v += guo_source<S>(q, cp, u);
+        f[q] = v;
+    }
+    rho_out = rho;
+}
+
+// second moments sum_q e_qa e_qb g_q of g = f - feq, packed (xx, yy, zz, xy,
+// xz, yz) (lettuce/_flow.py:228-234 applied to f - feq)
+template <class S, class R>
+LGB_HD void noneq_shear(const R (&f)[S::Q], R rho, const R (&u)[3], R uu, R (&pi)[6]) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) pi[k] = R(0);
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        const R g = f[q] - feq_q<S>(q, rho, u, uu);
+        const int ex = S::e(q, 0), ey = S::D > 1 ? S::e(q, 1) : 0,
+                  ez = S::D > 2 ? S::e(q, 2) : 0;
+        if (ex) pi[0] += g;
+        if (ey) pi[1] += g;
+        if (ez) pi[2] += g;
+        if (ex * ey == 1) pi[3] += g; else if (ex * ey == -1) pi[3] -= g;
+        if (ex * ez == 1) pi[4] += g; else if (ex * ez == -1) pi[4] -= g;
+        if (ey * ez == 1) pi[5] += g; else if (ey * ez == -1) pi[5] -= g;
+    }
+}
+
+// regularized: f <- feq + (1 - 1/tau) w_q Q_q : Pi_neq / (2 cs^4), with
+// Q_q,ab = e_qa e_qb - cs^2 delta_ab (regularized_collision.py:35-47)
+template <class S, class R>
+LGB_HD void collide_regularized(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+    R rho, u[3];
+    cell_moments<S>(f, rho, u);
+    const R uu = dot_uu<S>(u);
+    R pi[6];
+    noneq_shear<S>(f, rho, u, uu, pi);
+    const R third = R(1.0 / 3.0);
+    const R trace = pi[0] + pi[1] + pi[2];
+    const R k = (R(1) - R(cp.omega)) * R(4.5);  // (1 - 1/tau) / (2 cs^4)
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        const int ex = S::e(q, 0), ey = S::D > 1 ? S::e(q, 1) : 0,
+                  ez = S::D > 2 ? S::e(q, 2) : 0;
+        R qp = -third * trace;
+        if (ex) qp += pi[0];
+        if (ey) qp += pi[1];
+        if (ez) qp += pi[2];
+        const int xy = ex * ey, xz = ex * ez, yz = ey * ez;
+        if (xy) qp += R(2 * xy) * pi[3];
+        if (xz) qp += R(2 * xz) * pi[4];
+        if (yz) qp += R(2 * yz) * pi[5];
+        f[q] = feq_q<S>(q, rho, u, uu) + k * R(S::w(q)) * qp;
+    }
+    rho_out = rho;
+}
+
+// Smagorinsky: BGK with tau_eff from two fixed-point iterations of
+// nu_eff = (tau - 1/2) / 3 + C^2 S:S, S = Pi_neq / (2 rho cs^2 tau_eff)
+// (smagorinsky_collision.py:22-41), plus the optional force
+template <class S, class R>
+LGB_HD void collide_smagorinsky(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+    R rho, u[3];
+    forced_velocity<S>(f, cp, rho, u);
+    const R uu = dot_uu<S>(u);
+    R pi[6];
+    noneq_shear<S>(f, rho, u, uu, pi);
+    const R scale = R(1.5) / rho;  // 1 / (2 rho cs^2)
+    // S:S of the symmetric tensor with the off-diagonal entries counted twice
+    R ss = R(0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ss += (pi[k] * scale) * (pi[k] * scale);
+#pragma unroll
+    for (int k = 3; k < 6; ++k) ss += R(2) * (pi[k] * scale) * (pi[k] * scale);
+    const R tau = R(cp.tau);
+    const R nu = (tau - R(0.5)) / R(3);
+    R tau_eff = tau;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const R nu_eff = nu + R(cp.smag_c2) * ss / (tau_eff * tau_eff);
+        tau_eff = nu_eff * R(3) + R(0.5);
+    }
+    const R om = R(1) / tau_eff;
+    const bool src = cp.src_scale != 0.0;
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        R v = f[q] - om * (f[q] - feq_q<S>(q, rho, u, uu));
+        if (src) v += guo_source<S>(q, cp, u);
+        f[q] = v;
+    }
+    rho_out = rho;
+}
+
+// Per-launch tables of a collision, passed by value as a kernel parameter
+// (constant bank: the moment transforms read them as instruction operands).
+// Only MRT has any.
+struct NoTables {};
+template <int Q, class R> struct MrtTables {
+    R M[Q * Q];      // moment matrix, row-major
+    R Minv[Q * Q];   // its inverse
+    R inv_s[Q];      // 1 / relaxation time of each moment
+    int32_t eq;      // LGB_MRT_EQ_*
+};
+template <int COLL, class S, class R> struct TablesOf { using type = NoTables; };
+template <class S, class R> struct TablesOf<LGB_MRT, S, R> { using type = MrtTables<S::Q, R>; };
+
+// MRT: m = M f, m <- m - (m - meq) / s, f = M^-1 m
+template <class S, class R>
+LGB_HD void collide_mrt(R (&f)[S::Q], const MrtTables<S::Q, R> &t, R &rho_out) {
+    constexpr int Q = S::Q;
+    R m[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        R acc = R(0);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) acc += t.M[i * Q + q] * f[q];
+        m[i] = acc;
+    }
+    R meq[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) meq[i] = R(0);
+    const R rho = m[0];
+    if (t.eq == LGB_MRT_EQ_GENERIC) {
+        // Transform.equilibrium: the moments of feq(rho, u) of the populations
+        R r, u[3];
+        cell_moments<S>(f, r, u);
+        const R uu = dot_uu<S>(u);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const R e = feq_q<S>(q, r, u, uu);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) meq[i] += t.M[i * Q + q] * e;
+        }
+    } else if constexpr (Q == 9) {
+        const R jx = m[1], jy = m[2];
+        meq[0] = rho; meq[1] = jx; meq[2] = jy;
+        if (t.eq == LGB_MRT_EQ_DELLAR) {            // moments.py:180-204
+            meq[3] = jx * jx / rho * R(9) / R(2);
+            meq[4] = jx * jy / rho * R(9);
+            meq[5] = jy * jy / rho * R(9) / R(2);
+        } else {                                    // Lallemand & Luo, moments.py:240-274
+            const R jj = jx * jx + jy * jy;
+            meq[3] = R(1.0 / 2.0 * (2.0 / 3.0)) * (jx * jx - jy * jy);
+            meq[4] = R(1.0 / 2.0 * (2.0 / 3.0)) * (jx * jy);
+            meq[5] = R(1.0 / 4.0 * -8.0) * rho + R(1.0 / 6.0 * 18.0) * jj;
+            meq[6] = R(1.0 / 2.0 * -2.0) * jx;
+            meq[7] = R(1.0 / 2.0 * -2.0) * jy;
+            meq[8] = R(1.0 / 4.0 * 4.0) * rho + R(1.0 / 6.0 * -18.0) * jj;
+        }
+    } else if constexpr (Q == 27) {                 // Hermite, moments.py:511-545
+        const R jx = m[1], jy = m[2], jz = m[3];
+        const R r2 = rho * rho, r3 = r2 * rho, r4 = r3 * rho, r5 = r4 * rho;
+        meq[0] = rho; meq[1] = jx; meq[2] = jy; meq[3] = jz;
+        meq[4] = jx * jx / rho; meq[5] = jx * jy / rho; meq[6] = jx * jz / rho;
+        meq[7] = jy * jy / rho; meq[8] = jy * jz / rho; meq[9] = jz * jz / rho;
+        meq[10] = jx * jx * jy / r2; meq[11] = jx * jx * jz / r2;
+        meq[12] = jx * jy * jy / r2; meq[13] = jx * jy * jz / r2;
+        meq[14] = jx * jz * jz / r2; meq[15] = jy * jy * jz / r2;
+        meq[16] = jy * jz * jz / r2;
+        meq[17] = jx * jx * jy * jy / r3; meq[18] = jx * jx * jy * jz / r3;
+        meq[19] = jx * jx * jz * jz / r3; meq[20] = jx * jy * jy * jz / r3;
+        meq[21] = jx * jy * jz * jz / r3; meq[22] = jy * jy * jz * jz / r3;
+        meq[23] = jx * jx * jy * jy * jz / r4; meq[24] = jx * jx * jy * jz * jz / r4;
+        meq[25] = jx * jy * jy * jz * jz / r4;
+        meq[26] = jx * jy * jx * jz * jy * jz / r5;
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) m[i] = m[i] - t.inv_s[i] * (m[i] - meq[i]);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        R acc = R(0);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) acc += t.Minv[q * Q + i] * m[i];
+        f[q] = acc;
+    }
+    rho_out = rho;
+}
+
+template <int COLL, class S, class R, class TT = NoTables>
+LGB_HD void collide(R (&f)[S::Q], const CollideParams &cp, R &rho_out, const TT &tab = TT()) {
     if constexpr (COLL == LGB_BGK) {
         collide_bgk<S>(f, cp, rho_out);
     } else if constexpr (COLL == LGB_TRT) {
         collide_trt<S>(f, cp, rho_out);
     } else if constexpr (COLL == LGB_KBC) {
         collide_kbc<S>(f, cp, rho_out);
+    } else if constexpr (COLL == LGB_BGK_FORCED) {
+        collide_bgk_forced<S>(f, cp, rho_out);
+    } else if constexpr (COLL == LGB_REGULARIZED) {
+        collide_regularized<S>(f, cp, rho_out);
+    } else if constexpr (COLL == LGB_SMAGORINSKY) {
+        collide_smagorinsky<S>(f, cp, rho_out);
+    } else if constexpr (COLL == LGB_MRT) {
+        collide_mrt<S>(f, tab, rho_out);
     } else {
         R r = R(0);
 #pragma unroll

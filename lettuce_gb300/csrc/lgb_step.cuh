@@ -63,6 +63,9 @@ struct SubParams {
 struct StepParams {
     const void *f_in;
     void *f_out;
+    // MRT tables in host memory (read by the launch, not by the kernel)
+    const double *mrt_host;
+    int32_t mrt_eq;
     uint32_t X, Y, Z, N;
     FastDiv divZ, divY;
     CollideParams cp;
@@ -161,12 +164,12 @@ __device__ __forceinline__ SubParams select_sub(const StepParams &p, int idx) {
 }
 
 // substep `sb` (collision, bounce-back, equilibrium BC or none) at one cell
-template <class S, int COLL, class R>
+template <class S, int COLL, class R, class TT>
 __device__ __forceinline__ void apply_local_substep(const StepParams &p, const SubParams &sb,
-                                                    const Nbr &c, R (&f)[S::Q]) {
+                                                    const Nbr &c, R (&f)[S::Q], const TT &tab) {
     if (sb.kind == LGB_SUB_COLLISION) {
         R r;
-        collide<COLL, S>(f, p.cp, r);
+        collide<COLL, S>(f, p.cp, r, tab);
     } else if (sb.kind == LGB_SUB_BOUNCE_BACK) {
         // bounce_back_boundary.py:17-18: f <- f[opposite]
 #pragma unroll
@@ -213,9 +216,9 @@ __device__ __forceinline__ uint32_t coord_along(const Nbr &c, int axis) {
 // (equilibrium_outlet_p.py:61-71). The neighbour one cell inside is rebuilt
 // as the collide phase sees it at substep abb_k (its populations after the
 // substeps before abb_k).
-template <class S, int COLL, int LOAD, bool MASKED, class Sto>
+template <class S, int COLL, int LOAD, bool MASKED, class Sto, class TT>
 __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename Sto::T *__restrict__ fin,
-                                             const Nbr &c, typename Sto::R (&f)[S::Q]) {
+                                             const Nbr &c, typename Sto::R (&f)[S::Q], const TT &tab) {
     using R = typename Sto::R;
     uint32_t xn = c.x, yn = c.y, zn = c.z;
     if (p.abb_axis == 0) xn = p.abb_nb; else if (p.abb_axis == 1) yn = p.abb_nb; else zn = p.abb_nb;
@@ -227,7 +230,7 @@ __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename
     R g[S::Q];
     load_cell<S, Sto, LOAD, MASKED>(p, fin, cn, nn, nsb, g);
     const int idx = fl & LGB_FLAG_INDEX_MASK;
-    if (idx < p.abb_k) apply_local_substep<S, COLL>(p, select_sub(p, idx), cn, g);
+    if (idx < p.abb_k) apply_local_substep<S, COLL>(p, select_sub(p, idx), cn, g, tab);
     R rho, u[3], rn, un[3];
     cell_moments<S>(g, rn, un);
     if (p.abb_kind == LGB_SUB_EQUILIBRIUM_OUTLET_P) {
@@ -264,8 +267,9 @@ __device__ __forceinline__ void store_value(typename Sto::T *ptr, typename Sto::
 // anti-bounce-back outlet plane (when there is one); 2 = the outlet plane
 // only (one thread per plane cell). Splitting the outlet off keeps its extra
 // neighbour reconstruction out of the register budget of the bulk launch.
-template <int SID, int ST, int COLL, int PAT, int MASK>
-__global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
+// The step of one cell; the kernels below wrap it with their launch bounds.
+template <int SID, int ST, int COLL, int PAT, int MASK, class TT>
+__device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     using S = Stencil<SID>;
     using Sto = Storage<ST>;
     using R = typename Sto::R;
@@ -320,7 +324,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     } else if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
         if constexpr (MASK == 1) {
             // a cell off the outlet plane runs the substep its index names
-            apply_local_substep<S, COLL>(p, select_sub(p, fl & LGB_FLAG_INDEX_MASK), c, f);
+            apply_local_substep<S, COLL>(p, select_sub(p, fl & LGB_FLAG_INDEX_MASK), c, f, tab);
         } else if constexpr (MASK == 2) {
             // an outlet-plane cell runs the substep its index names and the
             // outlet substep, in sequence order
@@ -330,13 +334,13 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
 #pragma unroll 1
             for (int phase = 0; phase < 2; ++phase) {
                 if (phase != outlet_phase && idx != p.abb_k)
-                    apply_local_substep<S, COLL>(p, select_sub(p, idx), c, f);
+                    apply_local_substep<S, COLL>(p, select_sub(p, idx), c, f, tab);
                 if (phase == outlet_phase && outlet)
-                    apply_outlet<S, COLL, LOAD, MASKED, Sto>(p, fin, c, f);
+                    apply_outlet<S, COLL, LOAD, MASKED, Sto>(p, fin, c, f, tab);
             }
         } else {
             R r;
-            collide<COLL, S>(f, p.cp, r);
+            collide<COLL, S>(f, p.cp, r, tab);
         }
     }
 
@@ -377,6 +381,48 @@ __global__ void __launch_bounds__(256) step_kernel(const StepParams p) {
     }
 }
 
+// Only a block-size bound: a minimum-blocks bound of 1 lets the compiler
+// take more registers (the D3Q19 float32 pull kernel went from 48 to 72
+// registers and lost 11 %).
+template <int SID, int ST, int COLL>
+using StepTables = typename TablesOf<COLL, Stencil<SID>, typename Storage<ST>::R>::type;
+
+template <int SID, int ST, int COLL, int PAT, int MASK>
+__global__ void __launch_bounds__(256)
+step_kernel(const __grid_constant__ StepParams p, const __grid_constant__ StepTables<SID, ST, COLL> tab) {
+    step_cell<SID, ST, COLL, PAT, MASK>(p, tab);
+}
+
+// The D3Q27 KBC bulk kernels are held to 64 registers (4 blocks per SM):
+// measured on the 512x128x128 obstacle, 22.7k MLUPS against 17.1k with the
+// compiler's 80-103 registers, despite a few spilled values.
+#ifndef LGB_KBC_MIN_BLOCKS
+#define LGB_KBC_MIN_BLOCKS 4
+#endif
+template <int SID, int ST, int COLL, int PAT, int MASK>
+__global__ void __launch_bounds__(256, LGB_KBC_MIN_BLOCKS)
+step_kernel_bounded(const __grid_constant__ StepParams p,
+                    const __grid_constant__ StepTables<SID, ST, COLL> tab) {
+    step_cell<SID, ST, COLL, PAT, MASK>(p, tab);
+}
+
+// the collision's tables for one launch, from the host copy the caller gave
+template <int SID, int ST, int COLL>
+StepTables<SID, ST, COLL> make_tables(const StepParams &p) {
+    StepTables<SID, ST, COLL> t{};
+    if constexpr (COLL == LGB_MRT) {
+        using R = typename Storage<ST>::R;
+        constexpr int Q = Stencil<SID>::Q;
+        for (int i = 0; i < Q * Q; ++i) {
+            t.M[i] = R(p.mrt_host[i]);
+            t.Minv[i] = R(p.mrt_host[Q * Q + i]);
+        }
+        for (int i = 0; i < Q; ++i) t.inv_s[i] = R(1.0 / p.mrt_host[2 * Q * Q + i]);
+        t.eq = p.mrt_eq;
+    }
+    return t;
+}
+
 template <int SID, int ST, int COLL, int PAT, int MASK>
 cudaError_t launch_step(const StepParams &p, cudaStream_t stream) {
     const unsigned threads = 256;
@@ -386,7 +432,11 @@ cudaError_t launch_step(const StepParams &p, cudaStream_t stream) {
         count = p.N / ax;
     }
     const unsigned blocks = (unsigned)((count + threads - 1) / threads);
-    step_kernel<SID, ST, COLL, PAT, MASK><<<blocks, threads, 0, stream>>>(p);
+    const StepTables<SID, ST, COLL> tab = make_tables<SID, ST, COLL>(p);
+    if constexpr (COLL == LGB_KBC && SID == LGB_D3Q27 && MASK != 2)
+        step_kernel_bounded<SID, ST, COLL, PAT, MASK><<<blocks, threads, 0, stream>>>(p, tab);
+    else
+        step_kernel<SID, ST, COLL, PAT, MASK><<<blocks, threads, 0, stream>>>(p, tab);
     return cudaGetLastError();
 }
 
@@ -411,41 +461,55 @@ cudaError_t launch_step_set(const StepParams &p, cudaStream_t s) {
     }
 }
 
-template <int SID, int ST, int PAT, bool MASKED>
+// EXT = false: the ABI's base collisions (none, BGK, TRT, KBC); EXT = true:
+// forced BGK, regularized, Smagorinsky and MRT. The two sets are instantiated in
+// separate translation units so the build compiles them in parallel.
+template <int SID, int ST, int PAT, bool MASKED, bool EXT>
 cudaError_t dispatch_collision(int coll, const StepParams &p, cudaStream_t s) {
     if constexpr (PAT == LGB_STREAM_ONLY || PAT == LGB_AA_UNPACK) {
-        return launch_step_set<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+        if constexpr (EXT) return cudaErrorInvalidValue;
+        else return launch_step_set<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+    } else if constexpr (EXT) {
+        switch (coll) {
+        case LGB_BGK_FORCED: return launch_step_set<SID, ST, LGB_BGK_FORCED, PAT, MASKED>(p, s);
+        case LGB_REGULARIZED: return launch_step_set<SID, ST, LGB_REGULARIZED, PAT, MASKED>(p, s);
+        case LGB_SMAGORINSKY: return launch_step_set<SID, ST, LGB_SMAGORINSKY, PAT, MASKED>(p, s);
+        case LGB_MRT: return launch_step_set<SID, ST, LGB_MRT, PAT, MASKED>(p, s);
+        }
+        return cudaErrorInvalidValue;
     } else {
-    switch (coll) {
-    case LGB_NO_COLLISION: return launch_step_set<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
-    case LGB_BGK: return launch_step_set<SID, ST, LGB_BGK, PAT, MASKED>(p, s);
-    case LGB_TRT: return launch_step_set<SID, ST, LGB_TRT, PAT, MASKED>(p, s);
-    case LGB_KBC:
-        if constexpr (has_kbc<SID>()) return launch_step_set<SID, ST, LGB_KBC, PAT, MASKED>(p, s);
-        return cudaErrorNotSupported;
-    }
-    return cudaErrorInvalidValue;
+        switch (coll) {
+        case LGB_NO_COLLISION: return launch_step_set<SID, ST, LGB_NO_COLLISION, PAT, MASKED>(p, s);
+        case LGB_BGK: return launch_step_set<SID, ST, LGB_BGK, PAT, MASKED>(p, s);
+        case LGB_TRT: return launch_step_set<SID, ST, LGB_TRT, PAT, MASKED>(p, s);
+        case LGB_KBC:
+            if constexpr (has_kbc<SID>()) return launch_step_set<SID, ST, LGB_KBC, PAT, MASKED>(p, s);
+            return cudaErrorNotSupported;
+        }
+        return cudaErrorInvalidValue;
     }
 }
 
-template <int SID, int ST, bool MASKED>
+template <int SID, int ST, bool MASKED, bool EXT>
 cudaError_t dispatch_pattern(int coll, int pat, const StepParams &p, cudaStream_t s) {
     switch (pat) {
-    case LGB_PULL: return dispatch_collision<SID, ST, LGB_PULL, MASKED>(coll, p, s);
-    case LGB_PUSH: return dispatch_collision<SID, ST, LGB_PUSH, MASKED>(coll, p, s);
-    case LGB_LOCAL: return dispatch_collision<SID, ST, LGB_LOCAL, MASKED>(coll, p, s);
-    case LGB_AA_EVEN: return dispatch_collision<SID, ST, LGB_AA_EVEN, MASKED>(coll, p, s);
-    case LGB_AA_ODD: return dispatch_collision<SID, ST, LGB_AA_ODD, MASKED>(coll, p, s);
-    case LGB_STREAM_ONLY: return dispatch_collision<SID, ST, LGB_STREAM_ONLY, MASKED>(coll, p, s);
+    case LGB_PULL: return dispatch_collision<SID, ST, LGB_PULL, MASKED, EXT>(coll, p, s);
+    case LGB_PUSH: return dispatch_collision<SID, ST, LGB_PUSH, MASKED, EXT>(coll, p, s);
+    case LGB_LOCAL: return dispatch_collision<SID, ST, LGB_LOCAL, MASKED, EXT>(coll, p, s);
+    case LGB_AA_EVEN: return dispatch_collision<SID, ST, LGB_AA_EVEN, MASKED, EXT>(coll, p, s);
+    case LGB_AA_ODD: return dispatch_collision<SID, ST, LGB_AA_ODD, MASKED, EXT>(coll, p, s);
+    case LGB_STREAM_ONLY:
+        return dispatch_collision<SID, ST, LGB_STREAM_ONLY, MASKED, EXT>(coll, p, s);
     case LGB_AA_UNPACK:
-        if constexpr (!MASKED) return dispatch_collision<SID, ST, LGB_AA_UNPACK, false>(coll, p, s);
+        if constexpr (!MASKED) return dispatch_collision<SID, ST, LGB_AA_UNPACK, false, EXT>(coll, p, s);
         return cudaErrorInvalidValue;
     }
     return cudaErrorInvalidValue;
 }
 
-// one translation unit per (stencil, storage): lgb_step_<stencil>.cu built
-// with -DLGB_STORAGE_ID=<storage>
+// two translation units per (stencil, storage): lgb_step_<stencil>.cu built
+// with -DLGB_STORAGE_ID=<storage> and -DLGB_EXT_COLLISIONS=0 (step_*) or 1
+// (stepx_*)
 #define LGB_DECLARE_STEP(name)                                                              \
     cudaError_t name##_s0(int, int, bool, const StepParams &, cudaStream_t);              \
     cudaError_t name##_s1(int, int, bool, const StepParams &, cudaStream_t);              \
@@ -456,6 +520,11 @@ LGB_DECLARE_STEP(step_d2q9)
 LGB_DECLARE_STEP(step_d3q15)
 LGB_DECLARE_STEP(step_d3q19)
 LGB_DECLARE_STEP(step_d3q27)
+LGB_DECLARE_STEP(stepx_d1q3)
+LGB_DECLARE_STEP(stepx_d2q9)
+LGB_DECLARE_STEP(stepx_d3q15)
+LGB_DECLARE_STEP(stepx_d3q19)
+LGB_DECLARE_STEP(stepx_d3q27)
 #undef LGB_DECLARE_STEP
 
 }  // namespace lgb

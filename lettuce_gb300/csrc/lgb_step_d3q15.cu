@@ -7,14 +7,24 @@
 #ifndef LGB_STORAGE_ID
 #error "compile with -DLGB_STORAGE_ID=<storage>"
 #endif
+#ifndef LGB_EXT_COLLISIONS
+#define LGB_EXT_COLLISIONS 0
+#endif
 #define LGB_CAT2(a, b) a##b
 #define LGB_CAT(a, b) LGB_CAT2(a, b)
 
 namespace lgb {
+#if LGB_EXT_COLLISIONS
+cudaError_t LGB_CAT(stepx_d3q15_s, LGB_STORAGE_ID)(int coll, int pat, bool masked,
+                                                   const StepParams &p, cudaStream_t s) {
+    return masked ? dispatch_pattern<LGB_D3Q15, LGB_STORAGE_ID, true, true>(coll, pat, p, s)
+                  : dispatch_pattern<LGB_D3Q15, LGB_STORAGE_ID, false, true>(coll, pat, p, s);
+}
+#else
 cudaError_t LGB_CAT(step_d3q15_s, LGB_STORAGE_ID)(int coll, int pat, bool masked,
                                                   const StepParams &p, cudaStream_t s) {
-    return masked ? dispatch_pattern<LGB_D3Q15, LGB_STORAGE_ID, true>(coll, pat, p, s)
-                  : dispatch_pattern<LGB_D3Q15, LGB_STORAGE_ID, false>(coll, pat, p, s);
+    return masked ? dispatch_pattern<LGB_D3Q15, LGB_STORAGE_ID, true, false>(coll, pat, p, s)
+                  : dispatch_pattern<LGB_D3Q15, LGB_STORAGE_ID, false, false>(coll, pat, p, s);
 }
 #if LGB_STORAGE_ID >= 2
 cudaError_t LGB_CAT(step_vec2_d3q15_s, LGB_STORAGE_ID)(int coll, int pat, const StepParams &p,
@@ -22,4 +32,5 @@ cudaError_t LGB_CAT(step_vec2_d3q15_s, LGB_STORAGE_ID)(int coll, int pat, const 
     return dispatch_vec2<LGB_D3Q15, LGB_STORAGE_ID>(coll, pat, p, s);
 }
 #endif
+#endif  // LGB_EXT_COLLISIONS
 }  // namespace lgb

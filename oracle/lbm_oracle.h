@@ -16,6 +16,10 @@
  *   BGK             lettuce/ext/_collision/bgk_collision.py:17-22
  *   TRT             lettuce/ext/_collision/trt_collision.py:16-27
  *   KBC             lettuce/ext/_collision/kbc_collision.py:22-160
+ *   regularized     lettuce/ext/_collision/regularized_collision.py:17-47
+ *   Smagorinsky     lettuce/ext/_collision/smagorinsky_collision.py:22-41
+ *   forces          lettuce/ext/_force/guo.py:17-36, shan_chen.py:13-24
+ *   MRT             lettuce/ext/_collision/mrt_collision.py:23-30
  *   bounce-back     lettuce/ext/_boundary/bounce_back_boundary.py:17-18
  *   equilibrium BC  lettuce/ext/_boundary/equilibrium_boundary_pu.py:79-84
  *   anti-bounce-back outlet
@@ -39,7 +43,13 @@ extern "C" {
 /* stencil ids (same numbering as the CUDA library) */
 enum { ORC_D1Q3 = 1, ORC_D2Q9 = 2, ORC_D3Q15 = 3, ORC_D3Q19 = 4, ORC_D3Q27 = 5 };
 /* collision kinds */
-enum { ORC_NO_COLLISION = 0, ORC_BGK = 1, ORC_TRT = 2, ORC_KBC = 3 };
+enum { ORC_NO_COLLISION = 0, ORC_BGK = 1, ORC_TRT = 2, ORC_KBC = 3, ORC_REGULARIZED = 4,
+       ORC_SMAGORINSKY = 5, ORC_MRT = 6 };
+/* MRT equilibrium moments: lettuce/util/moments.py D2Q9Dellar (:180-204),
+ * D2Q9Lallemand (:240-274), D3Q27Hermite (:511-545) */
+enum { ORC_MRT_EQ_DELLAR = 1, ORC_MRT_EQ_LALLEMAND = 2, ORC_MRT_EQ_HERMITE = 3 };
+/* body forces (BGK and Smagorinsky) */
+enum { ORC_FORCE_NONE = 0, ORC_FORCE_GUO = 1, ORC_FORCE_SHAN_CHEN = 2 };
 /* substep kinds */
 enum { ORC_SUB_COLLISION = 0, ORC_SUB_BOUNCE_BACK = 1, ORC_SUB_EQUILIBRIUM_PU = 2,
        ORC_SUB_ANTI_BOUNCE_BACK = 3, ORC_SUB_NONE = 4, ORC_SUB_EQUILIBRIUM_OUTLET_P = 5,
@@ -77,6 +87,12 @@ typedef struct {
     int32_t n_sub;
     int32_t collision_index;
     const orc_substep *sub;  /* [n_sub] */
+    int32_t force;           /* ORC_FORCE_* */
+    double force_tau;
+    double accel[3];         /* lattice units */
+    double smagorinsky_constant;
+    int32_t mrt_equilibrium;
+    const double *mrt_tables; /* M [Q][Q], M^-1 [Q][Q], relaxation times [Q] */
 } orc_problem;
 
 int orc_stencil_dq(int stencil, int *d, int *q);

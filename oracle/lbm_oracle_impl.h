@@ -123,6 +123,44 @@ static void SFX(kbc_s)(const SFX(geom) *g, const REAL *fc, REAL *s)
     }
 }
 
+/* u + Force.u_eq: guo.py:30-34 (scale 1/2), shan_chen.py:19-22 (scale tau) */
+static void SFX(force_velocity)(const SFX(geom) *g, const orc_problem *p, REAL rho, REAL *u)
+{
+    if (p->force == ORC_FORCE_NONE) return;
+    const REAL scale = p->force == ORC_FORCE_GUO ? (REAL)0.5 : (REAL)(p->force_tau * 1);
+    for (int d = 0; d < g->d; ++d) u[d] = u[d] + scale * (REAL)p->accel[d] / rho;
+}
+
+/* Guo's source term, guo.py:17-28:
+ * (1 - 1/(2 tau)) w_q [(e_q - u)/cs^2 + (e_q.u) e_q/cs^4] . a */
+static void SFX(guo_source)(const SFX(geom) *g, const orc_problem *p, const REAL *u, REAL *si)
+{
+    const double cs = SFX(cs)();
+    const REAL cs2 = (REAL)(cs * cs), cs4 = (REAL)(pow(cs, 4));
+    for (int q = 0; q < g->q; ++q) {
+        REAL eu = 0;
+        for (int d = 0; d < g->d; ++d) eu += (REAL)g->st->e[q][d] * u[d];
+        REAL acc = 0;
+        for (int d = 0; d < g->d; ++d) {
+            const REAL e = (REAL)g->st->e[q][d];
+            acc += ((e - u[d]) / cs2 + e * eu / cs4) * (REAL)p->accel[d];
+        }
+        si[q] = (REAL)(1 - 1 / (2 * p->force_tau)) * ((REAL)g->st->w[q] * acc);
+    }
+}
+
+/* Pi_ab = sum_q e_qa e_qb g_q (lettuce/_flow.py:228-234) */
+static void SFX(shear_tensor)(const SFX(geom) *g, const REAL *gq, REAL pi[3][3])
+{
+    for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) pi[a][b] = 0;
+    for (int a = 0; a < g->d; ++a) for (int b = 0; b < g->d; ++b) {
+        REAL acc = 0;
+        for (int q = 0; q < g->q; ++q)
+            acc += gq[q] * (REAL)(g->st->e[q][a] * g->st->e[q][b]);
+        pi[a][b] = acc;
+    }
+}
+
 /* one collision at one cell, in place on fc[Q] */
 static void SFX(cell_collide)(const SFX(geom) *g, const orc_problem *p, REAL *fc)
 {
@@ -133,9 +171,118 @@ static void SFX(cell_collide)(const SFX(geom) *g, const orc_problem *p, REAL *fc
         return;
     case ORC_BGK: { /* lettuce/ext/_collision/bgk_collision.py:17-22 */
         SFX(cell_moments)(g, fc, &rho, u);
+        SFX(force_velocity)(g, p, rho, u);
         SFX(cell_feq)(g, rho, u, feq);
         const REAL omega = (REAL)(1.0 / p->tau);
-        for (int q = 0; q < Q; ++q) fc[q] = fc[q] - omega * (fc[q] - feq[q]);
+        REAL si[27] = {0};
+        if (p->force == ORC_FORCE_GUO) SFX(guo_source)(g, p, u, si);
+        for (int q = 0; q < Q; ++q) fc[q] = fc[q] - omega * (fc[q] - feq[q]) + si[q];
+        return;
+    }
+    case ORC_REGULARIZED: { /* lettuce/ext/_collision/regularized_collision.py:17-47 */
+        const double cs = SFX(cs)();
+        const REAL cs2 = (REAL)(cs * cs), cs4 = (REAL)pow(cs, 4);
+        SFX(cell_moments)(g, fc, &rho, u);
+        SFX(cell_feq)(g, rho, u, feq);
+        REAL gq[27] = {0}, pi[3][3];
+        for (int q = 0; q < Q; ++q) gq[q] = fc[q] - feq[q];
+        SFX(shear_tensor)(g, gq, pi);
+        for (int q = 0; q < Q; ++q) {
+            REAL acc = 0;
+            for (int a = 0; a < g->d; ++a) for (int b = 0; b < g->d; ++b) {
+                REAL qm = (REAL)(g->st->e[q][a] * g->st->e[q][b]);
+                if (a == b) qm -= cs2;
+                acc += qm * pi[a][b];
+            }
+            const REAL fi1 = (REAL)g->st->w[q] * acc / (2 * cs4);
+            fc[q] = feq[q] + (1 - (REAL)(1.0 / p->tau)) * fi1;
+        }
+        return;
+    }
+    case ORC_MRT: { /* lettuce/ext/_collision/mrt_collision.py:23-30 */
+        const double *M = p->mrt_tables, *Mi = M + Q * Q, *sr = Mi + Q * Q;
+        REAL m[27], meq[27];
+        for (int i = 0; i < Q; ++i) {
+            REAL acc = 0;
+            for (int q = 0; q < Q; ++q) acc += (REAL)M[i * Q + q] * fc[q];
+            m[i] = acc;
+            meq[i] = 0;
+        }
+        const REAL rho = m[0];
+        if (p->mrt_equilibrium == ORC_MRT_EQ_DELLAR) {
+            const REAL jx = m[1], jy = m[2];
+            meq[0] = rho; meq[1] = jx; meq[2] = jy;
+            meq[3] = jx * jx / rho * 9 / 2;
+            meq[4] = jx * jy / rho * 9;
+            meq[5] = jy * jy / rho * 9 / 2;
+        } else if (p->mrt_equilibrium == ORC_MRT_EQ_LALLEMAND) {
+            const REAL jx = m[1], jy = m[2];
+            const REAL c1 = -2, alpha2 = -8, alpha3 = 4, gamma1 = (REAL)(2.0 / 3.0), gamma2 = 18,
+                       gamma3 = (REAL)(2.0 / 3.0), gamma4 = -18;
+            meq[0] = rho; meq[1] = jx; meq[2] = jy;
+            meq[3] = (REAL)0.5 * gamma1 * (jx * jx - jy * jy);
+            meq[4] = (REAL)0.5 * gamma3 * (jx * jy);
+            meq[5] = (REAL)0.25 * alpha2 * rho + (REAL)(1.0 / 6.0) * gamma2 * (jx * jx + jy * jy);
+            meq[6] = (REAL)0.5 * c1 * jx;
+            meq[7] = (REAL)0.5 * c1 * jy;
+            meq[8] = (REAL)0.25 * alpha3 * rho + (REAL)(1.0 / 6.0) * gamma4 * (jx * jx + jy * jy);
+        } else if (p->mrt_equilibrium == ORC_MRT_EQ_HERMITE) {
+            const REAL jx = m[1], jy = m[2], jz = m[3];
+            const REAL r2 = rho * rho, r3 = r2 * rho, r4 = r3 * rho, r5 = r4 * rho;
+            meq[0] = rho; meq[1] = jx; meq[2] = jy; meq[3] = jz;
+            meq[4] = jx * jx / rho; meq[5] = jx * jy / rho; meq[6] = jx * jz / rho;
+            meq[7] = jy * jy / rho; meq[8] = jy * jz / rho; meq[9] = jz * jz / rho;
+            meq[10] = jx * jx * jy / r2; meq[11] = jx * jx * jz / r2; meq[12] = jx * jy * jy / r2;
+            meq[13] = jx * jy * jz / r2; meq[14] = jx * jz * jz / r2; meq[15] = jy * jy * jz / r2;
+            meq[16] = jy * jz * jz / r2;
+            meq[17] = jx * jx * jy * jy / r3; meq[18] = jx * jx * jy * jz / r3;
+            meq[19] = jx * jx * jz * jz / r3; meq[20] = jx * jy * jy * jz / r3;
+            meq[21] = jx * jy * jz * jz / r3; meq[22] = jy * jy * jz * jz / r3;
+            meq[23] = jx * jx * jy * jy * jz / r4; meq[24] = jx * jx * jy * jz * jz / r4;
+            meq[25] = jx * jy * jy * jz * jz / r4;
+            meq[26] = jx * jy * jx * jz * jy * jz / r5;
+        } else { /* the moments of feq(rho, u) (Transform.equilibrium's intent) */
+            REAL r0, u0[3];
+            SFX(cell_moments)(g, fc, &r0, u0);
+            SFX(cell_feq)(g, r0, u0, feq);
+            for (int i = 0; i < Q; ++i) {
+                REAL acc = 0;
+                for (int q = 0; q < Q; ++q) acc += (REAL)M[i * Q + q] * feq[q];
+                meq[i] = acc;
+            }
+        }
+        for (int i = 0; i < Q; ++i) m[i] = m[i] - (REAL)(1.0 / sr[i]) * (m[i] - meq[i]);
+        for (int q = 0; q < Q; ++q) {
+            REAL acc = 0;
+            for (int i = 0; i < Q; ++i) acc += (REAL)Mi[q * Q + i] * m[i];
+            fc[q] = acc;
+        }
+        return;
+    }
+    case ORC_SMAGORINSKY: { /* lettuce/ext/_collision/smagorinsky_collision.py:22-41 */
+        const double cs = SFX(cs)();
+        SFX(cell_moments)(g, fc, &rho, u);
+        SFX(force_velocity)(g, p, rho, u);
+        SFX(cell_feq)(g, rho, u, feq);
+        REAL gq[27] = {0}, pi[3][3];
+        for (int q = 0; q < Q; ++q) gq[q] = fc[q] - feq[q];
+        SFX(shear_tensor)(g, gq, pi);
+        for (int a = 0; a < g->d; ++a) for (int b = 0; b < g->d; ++b)
+            pi[a][b] /= (REAL)(2.0 * rho * (cs * cs));
+        REAL tau_eff = (REAL)p->tau;
+        const REAL nu = ((REAL)p->tau - (REAL)0.5) / (REAL)3.0;
+        for (int it = 0; it < 2; ++it) {
+            REAL ss = 0;
+            for (int a = 0; a < g->d; ++a) for (int b = 0; b < g->d; ++b) {
+                const REAL sab = pi[a][b] / tau_eff;
+                ss += sab * sab;
+            }
+            const REAL nu_t = (REAL)(p->smagorinsky_constant * p->smagorinsky_constant) * ss;
+            tau_eff = (nu + nu_t) * (REAL)3.0 + (REAL)0.5;
+        }
+        REAL si[27] = {0};
+        if (p->force == ORC_FORCE_GUO) SFX(guo_source)(g, p, u, si);
+        for (int q = 0; q < Q; ++q) fc[q] = fc[q] - (REAL)1.0 / tau_eff * (fc[q] - feq[q]) + si[q];
         return;
     }
     case ORC_TRT: { /* lettuce/ext/_collision/trt_collision.py:16-27 */

@@ -36,7 +36,10 @@ _lock = threading.Lock()
 _lib = None
 
 STENCIL_IDS = {"D1Q3": 1, "D2Q9": 2, "D3Q15": 3, "D3Q19": 4, "D3Q27": 5}
-COLLISION_IDS = {"none": 0, "bgk": 1, "trt": 2, "kbc": 3}
+COLLISION_IDS = {"none": 0, "bgk": 1, "trt": 2, "kbc": 3, "regularized": 4, "smagorinsky": 5,
+                 "mrt": 6}
+MRT_EQ_IDS = {"generic": 0, "dellar": 1, "lallemand": 2, "hermite": 3}
+FORCE_IDS = {None: 0, "guo": 1, "shan_chen": 2}
 SUB_KIND = {"collision": 0, "bounce_back": 1, "equilibrium_pu": 2,
             "anti_bounce_back": 3, "none": 4, "equilibrium_outlet_p": 5,
             "partially_saturated": 6}
@@ -99,7 +102,13 @@ class _Problem(ctypes.Structure):
                 ("nsm", ctypes.c_void_p),
                 ("n_sub", ctypes.c_int32),
                 ("collision_index", ctypes.c_int32),
-                ("sub", ctypes.POINTER(_Sub))]
+                ("sub", ctypes.POINTER(_Sub)),
+                ("force", ctypes.c_int32),
+                ("force_tau", ctypes.c_double),
+                ("accel", ctypes.c_double * 3),
+                ("smagorinsky_constant", ctypes.c_double),
+                ("mrt_equilibrium", ctypes.c_int32),
+                ("mrt_tables", ctypes.c_void_p)]
 
 
 def build():
@@ -202,9 +211,13 @@ def assemble_masks(resolution, q, name, pre, post):
 
 def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
         strategy="POST_STREAMING", pre=(), post=(), nthreads=None,
-        masks=None):
+        masks=None, force=None, force_tau=1.0, accel=(0.0, 0.0, 0.0),
+        smagorinsky_constant=0.17, mrt=None):
     """Advance ``f`` ([Q, *res], float64 or float32) by ``nsteps`` steps and
-    return the new array; ``f`` is not modified."""
+    return the new array; ``f`` is not modified. ``force`` ("guo",
+    "shan_chen" or None) with ``force_tau`` and ``accel`` (lattice units)
+    applies to the BGK and Smagorinsky collisions. ``mrt`` = (equilibrium
+    name, M, M^-1, relaxation times) for the "mrt" collision."""
     L = lib()
     f = np.ascontiguousarray(f)
     dt = f.dtype
@@ -254,6 +267,19 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
     p.strategy = STRATEGY_IDS[strategy]
     p.tau = float(tau)
     p.tau_minus = float(tau_minus)
+    p.force = FORCE_IDS[force]
+    p.force_tau = float(force_tau)
+    for k, a in enumerate(list(accel)[:3]):
+        p.accel[k] = float(a)
+    p.smagorinsky_constant = float(smagorinsky_constant)
+    if mrt is not None:
+        eq, M, Mi, srel = mrt
+        tables = np.ascontiguousarray(np.concatenate(
+            [np.asarray(M, np.float64).ravel(), np.asarray(Mi, np.float64).ravel(),
+             np.asarray(srel, np.float64).ravel()]))
+        keep.append(tables)
+        p.mrt_equilibrium = MRT_EQ_IDS[eq]
+        p.mrt_tables = tables.ctypes.data
     if ncm is not None:
         ncm = np.ascontiguousarray(ncm, dtype=np.uint8)
         nsm = np.ascontiguousarray(nsm, dtype=np.uint8)

@@ -349,6 +349,85 @@ def case_adjoint():
     np.savez_compressed(os.path.join(OUT, "adjoint_d2q9_32.npz"), **out)
 
 
+def case_collision_ext(name, stencil, res, kind, steps, seed):
+    """random populations under the regularized / Smagorinsky collisions and
+    BGK with a Guo or Shan-Chen body force (PRE and POST streaming)"""
+    from lettuce.ext import Guo, ShanChen, RegularizedCollision, SmagorinskyCollision
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.2 * rng.standard_normal([st.q] + res))
+    tau, force_tau = 0.73, 0.81
+    accel = [1e-3, -4e-4, 6e-4][:len(res)]
+    out = {"f0": f0, "tau": np.float64(tau), "steps": np.int64(steps),
+           "force_tau": np.float64(force_tau), "accel": np.array(accel)}
+    for sname, strat in STRATS.items():
+        flow = GivenFlow(st, f0)
+        if kind == "regularized":
+            coll = RegularizedCollision(tau)
+            out["tau"] = np.float64(flow.units.relaxation_parameter_lu)
+        elif kind == "smagorinsky":
+            coll = SmagorinskyCollision(tau, smagorinsky_constant=0.3)
+        elif kind == "smagorinsky_guo":
+            coll = SmagorinskyCollision(tau, smagorinsky_constant=0.3,
+                                        force=Guo(flow, force_tau, accel))
+        elif kind == "bgk_guo":
+            coll = BGKCollision(tau, force=Guo(flow, force_tau, accel))
+        elif kind == "bgk_shanchen":
+            coll = BGKCollision(tau, force=ShanChen(flow, force_tau, accel))
+        sim = Simulation(flow, coll, [], streaming_strategy=strat)
+        sim(steps)
+        out[f"f_{sname}"] = npf(flow.f)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res, "kind": kind,
+                              "smagorinsky_constant": 0.3})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_poiseuille(name, force_kind, steps):
+    """lettuce's forced Poiseuille channel (tests/collision/test_force.py set-up:
+    PoiseuilleFlow2D 17^2, Re 1, Ma 0.02, BGK with Guo or Shan-Chen)"""
+    from lettuce.ext import Guo, ShanChen, PoiseuilleFlow2D
+    flow = PoiseuilleFlow2D(context=CTX, resolution=17, reynolds_number=1,
+                            mach_number=0.02, initialize_with_zeros=True)
+    a_lu = flow.units.convert_acceleration_to_lu(flow.acceleration)
+    tau = flow.units.relaxation_parameter_lu
+    F = Guo if force_kind == "guo" else ShanChen
+    force = F(flow=flow, tau=tau, acceleration=a_lu)
+    sim = Simulation(flow=flow, collision=BGKCollision(tau=tau, force=force), reporter=[])
+    f0 = npf(flow.f)
+    sim(steps)
+    out = {"f0": f0, "f_final": npf(flow.f), "tau": np.float64(tau),
+           "accel": npf(a_lu), "steps": np.int64(steps),
+           "u_final": npf(flow.u(acceleration=a_lu)),
+           "ncm": npf(sim.no_collision_mask).astype(np.uint8)}
+    out["meta"] = json.dumps({"force": force_kind, "res": [17, 17]})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def case_mrt(name, stencil, transform, res, steps, seed):
+    """random populations under lettuce's MRT collision with one of its
+    moment transforms and per-moment relaxation times (PRE and POST)"""
+    from lettuce.ext import MRTCollision
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.2 * rng.standard_normal([st.q] + res))
+    srel = 0.55 + 0.6 * rng.random(st.q)
+    srel[0] = 1.0
+    out = {"f0": f0, "steps": np.int64(steps), "relaxation": srel}
+    for sname, strat in STRATS.items():
+        flow = GivenFlow(st, f0)
+        t = transform(st, CTX)
+        sim = Simulation(flow, MRTCollision(t, srel.tolist(), CTX), [], streaming_strategy=strat)
+        sim(steps)
+        out[f"f_{sname}"] = npf(flow.f)
+        out["matrix"] = npf(t.matrix)
+        out["inverse"] = npf(t.inverse)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res,
+                              "transform": transform.__name__})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
 def main():
     torch.set_num_threads(os.cpu_count() or 1)
     case_tgv("tgv2d_d2q9_bgk", D2Q9, 16, 1000, "bgk", 5)
@@ -373,6 +452,18 @@ def main():
     case_outlet_p("outletp_d3q19_bgk", D3Q19, [20, 8, 8], 2.0, 1.01, 4)
     case_psm("psm_d2q9_bgk", D2Q9, [20, 16], 0.4, 5, 21)
     case_psm("psm_d3q19_bgk", D3Q19, [9, 8, 7], 0.7, 3, 22)
+    for stencil, res, seed0 in [(D2Q9, [7, 6], 40), (D3Q19, [5, 4, 4], 50),
+                                (D3Q27, [4, 4, 3], 60)]:
+        for k, kind in enumerate(["regularized", "smagorinsky", "smagorinsky_guo", "bgk_guo",
+                                  "bgk_shanchen"]):
+            case_collision_ext(f"ext_{stencil.__name__.lower()}_{kind}", stencil, res, kind, 3,
+                               seed0 + k)
+    from lettuce.util.moments import D2Q9Dellar, D2Q9Lallemand, D3Q27Hermite
+    case_mrt("mrt_d2q9_lallemand", D2Q9, D2Q9Lallemand, [7, 6], 3, 70)
+    case_mrt("mrt_d2q9_dellar", D2Q9, D2Q9Dellar, [7, 6], 3, 71)
+    case_mrt("mrt_d3q27_hermite", D3Q27, D3Q27Hermite, [4, 4, 3], 3, 72)
+    case_poiseuille("poiseuille_guo", "guo", 300)
+    case_poiseuille("poiseuille_shanchen", "shan_chen", 300)
     case_native_kats()
     case_observables()
     case_adjoint()

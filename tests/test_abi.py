@@ -36,9 +36,10 @@ def test_struct_layout_matches_header(tmp_path, lgb):
     src = tmp_path / "probe.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "lettuce_gb300.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(lgb_step_desc),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(lgb_step_desc),"
         " offsetof(lgb_step_desc, sub), offsetof(lgb_step_desc, options),"
-        " sizeof(lgb_substep), offsetof(lgb_substep, rho), offsetof(lgb_substep, u_stride));"
+        " sizeof(lgb_substep), offsetof(lgb_substep, rho), offsetof(lgb_substep, u_stride),"
+        " offsetof(lgb_step_desc, accel), offsetof(lgb_step_desc, smagorinsky_constant));"
         "return 0;}\n")
     exe = tmp_path / "probe"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)],
@@ -47,7 +48,8 @@ def test_struct_layout_matches_header(tmp_path, lgb):
                                           check=True).stdout.split()]
     S, D = _lib.Substep, _lib.StepDesc
     assert got == [ctypes.sizeof(D), D.sub.offset, D.options.offset, ctypes.sizeof(S),
-                   S.rho.offset, S.u_stride.offset]
+                   S.rho.offset, S.u_stride.offset, D.accel.offset,
+                   D.smagorinsky_constant.offset]
 
 
 def _desc(**kw):
@@ -74,6 +76,12 @@ def _desc(**kw):
     (dict(res=[0, 8]), "must be positive"),
     (dict(res=[70000, 70000]), "exceeds"),
     (dict(f_in=0), "NULL"),
+    (dict(collision=7), "unknown collision"),
+    (dict(collision=6), "MRT collision needs its tables"),
+    (dict(force=3), "unknown force"),
+    (dict(collision=2, tau_minus=1.0, force=1, force_tau=0.8), "needs the BGK or Smagorinsky"),
+    (dict(force=1, force_tau=0.0), "force's tau must be positive"),
+    (dict(options=4), "unknown option bits"),
 ])
 def test_step_validation_errors(lgb, kw, msg):
     from lettuce_gb300 import _lib

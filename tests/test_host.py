@@ -181,10 +181,36 @@ def test_no_cpu_path():
         sim(1)
 
 
-def test_force_has_no_kernel():
+def test_force_without_kernel_is_refused():
+    """a user force that offers no kernel is refused, not run in torch"""
+    class TorchOnlyForce(lt.Guo):
+        def native_available(self):
+            return False
+
     flow = lt.TaylorGreenVortex(lt.Context("cpu"), 8, 100, 0.05, lt.D2Q9)
     with pytest.raises(NotImplementedError):
-        lt.Simulation(flow, lt.BGKCollision(0.6, force=object()), [])
+        lt.Simulation(flow, lt.BGKCollision(0.6, force=TorchOnlyForce(flow, 0.6, [1e-4, 0])), [])
+
+
+def test_force_descriptors():
+    flow = lt.PoiseuilleFlow2D(CPU64, 17, 1, 0.02)
+    a = flow.units.convert_acceleration_to_lu(flow.acceleration)
+    tau = flow.units.relaxation_parameter_lu
+    for F, kind in [(lt.Guo, _lib.FORCE_GUO), (lt.ShanChen, _lib.FORCE_SHAN_CHEN)]:
+        sim = lt.Simulation(flow, lt.BGKCollision(tau, force=F(flow, 0.9, a)), [])
+        d = sim._desc
+        assert (d.collision, d.force, d.force_tau) == (_lib.BGK, kind, 0.9)
+        assert list(d.accel)[:2] == a.tolist()
+    g = lt.Guo(flow, 0.9, a)
+    assert g.ueq_scaling_factor == 0.5 and lt.ShanChen(flow, 0.9, a).ueq_scaling_factor == 0.9
+    # Guo's source term restated on torch tensors: zero acceleration, zero term
+    u = torch.zeros([2, 17, 17], dtype=torch.float64)
+    assert torch.count_nonzero(lt.Guo(flow, 0.9, [0.0, 0.0]).source_term(u)) == 0
+    sim = lt.Simulation(flow, lt.SmagorinskyCollision(0.7, smagorinsky_constant=0.2), [])
+    assert (sim._desc.collision, sim._desc.smagorinsky_constant) == (_lib.SMAGORINSKY, 0.2)
+    reg = lt.RegularizedCollision(0.6)
+    sim = lt.Simulation(flow, reg, [])
+    assert sim._desc.collision == _lib.REGULARIZED and sim._desc.tau == tau == reg.tau
 
 
 def test_checkpoint_round_trip(tmp_path):

@@ -138,3 +138,68 @@ def test_partially_saturated_cases(oracle, name, strategy):
     out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision="bgk",
                      tau=float(z["tau"]), strategy=strategy, post=post)
     assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+EXT_FORCE = {"bgk_guo": ("bgk", "guo"), "bgk_shanchen": ("bgk", "shan_chen"),
+             "smagorinsky_guo": ("smagorinsky", "guo"), "smagorinsky": ("smagorinsky", None),
+             "regularized": ("regularized", None)}
+
+
+@pytest.mark.parametrize("name", golden_names("ext_"))
+@pytest.mark.parametrize("strategy", STRATS)
+def test_forces_and_collisions(oracle, name, strategy):
+    """regularized and Smagorinsky collisions, BGK / Smagorinsky with Guo and
+    Shan-Chen forces (random fields, lettuce float64)"""
+    z = golden(name)
+    m = meta(z)
+    coll, force = EXT_FORCE[m["kind"]]
+    out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision=coll,
+                     tau=float(z["tau"]), strategy=strategy, force=force,
+                     force_tau=float(z["force_tau"]), accel=z["accel"],
+                     smagorinsky_constant=m["smagorinsky_constant"])
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", golden_names("poiseuille"))
+def test_poiseuille_force(oracle, name):
+    """lettuce's forced Poiseuille channel (bounce-back walls, Guo or
+    Shan-Chen), 300 POST_STREAMING steps"""
+    z = golden(name)
+    m = meta(z)
+    mask = np.zeros([17, 17], dtype=bool)
+    mask[:, [0, -1]] = True
+    post = [{"kind": "bounce_back", "mask": mask}]
+    ncm, _ = oracle.assemble_masks([17, 17], 9, "D2Q9", [], post)
+    assert np.array_equal(ncm, z["ncm"])
+    out = oracle.run("D2Q9", z["f0"], int(z["steps"]), collision="bgk", tau=float(z["tau"]),
+                     strategy="POST_STREAMING", post=post, force=m["force"],
+                     force_tau=float(z["tau"]), accel=z["accel"])
+    assert rel(out, z["f_final"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", golden_names("mrt_"))
+@pytest.mark.parametrize("strategy", STRATS)
+def test_mrt_cases(oracle, name, strategy):
+    """lettuce's MRT collision with its Lallemand, Dellar and Hermite moment
+    transforms (random fields, per-moment relaxation times, float64)"""
+    z = golden(name)
+    m = meta(z)
+    eq = {"D2Q9Lallemand": "lallemand", "D2Q9Dellar": "dellar",
+          "D3Q27Hermite": "hermite"}[m["transform"]]
+    out = oracle.run(m["stencil"], z["f0"], int(z["steps"]), collision="mrt",
+                     strategy=strategy, mrt=(eq, z["matrix"], z["inverse"], z["relaxation"]))
+    assert rel(out, z[f"f_{strategy}"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", golden_names("mrt_"))
+def test_moment_bases_are_lettuces(name):
+    """the package builds each basis from its polynomials in e and inverts it;
+    the result equals lettuce's tabulated matrices"""
+    import lettuce_gb300 as lt
+    import torch
+    z = golden(name)
+    m = meta(z)
+    T = getattr(lt, m["transform"])
+    t = T(getattr(lt, m["stencil"])(), lt.Context("cpu", torch.float64))
+    assert np.max(np.abs(t.matrix_np - z["matrix"])) < 1e-15
+    assert np.max(np.abs(t.inverse_np - z["inverse"])) < 1e-14
