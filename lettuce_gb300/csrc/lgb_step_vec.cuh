@@ -8,8 +8,8 @@
 // f32x2 instructions (lgb_shifted.cuh), bit-identical to the one-cell path.
 //
 // Patterns: PULL, PUSH, LOCAL, AA_EVEN, AA_ODD. PUSH and AA_ODD store a
-// shifted pair as two 16-bit stores (each half is written by exactly one
-// thread, so there is no race).
+// shifted pair through a lane shuffle as whole words, and as 16-bit halves
+// at row ends and warp edges (each half is written by exactly one thread).
 #pragma once
 
 #include "lgb_shifted.cuh"
@@ -48,17 +48,17 @@ __device__ __forceinline__ uint32_t load_pair(const uint32_t *__restrict__ row, 
     return __byte_perm(__ldg(row + tz), __ldg(row + tzp), 0x5432);
 }
 
-// four resident blocks per SM (64 registers): occupancy hides the load latency
-// better than the registers the compiler would otherwise spend
+// the step of cell pair t (cells 2t, 2t + 1 of the grid p, t < N / 2);
+// p.divZ holds Z / 2. For PUSH and AA_ODD, pair t must be held by lane
+// t mod 32 of a warp whose active lanes are `lanes`.
 template <int SID, int ST, int COLL, int PAT>
-__global__ void __launch_bounds__(256, 4) step_vec2_kernel(const StepParams p) {
+__device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
+                                          const unsigned lanes = 0xffffffffu) {
     using S = Stencil<SID>;
     using P = Pack16<ST>;
     const uint32_t Zh = p.Z >> 1;
     const uint32_t Nh = p.N >> 1;
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= Nh) return;
-    const uint32_t row = p.divZ.div(t);  // divZ holds Z/2 here
+    const uint32_t row = p.divZ.div(t);
     const uint32_t tz = t - row * Zh;
     const uint32_t x = p.divY.div(row);
     const uint32_t y = row - x * p.Y;
@@ -109,15 +109,50 @@ __global__ void __launch_bounds__(256, 4) step_vec2_kernel(const StepParams p) {
             if (dz == 0) {
                 r[tz] = w;
             } else {
+                // the shifted pair straddles two words. A word whose two
+                // halves come from pairs held by neighbouring lanes of one
+                // row is composed by a shuffle and stored whole; at a row end
+                // or a warp edge each half is stored alone by the lane that
+                // holds its value (every half is written exactly once)
                 unsigned short *r16 = reinterpret_cast<unsigned short *>(r);
-                const uint32_t z0 = 2 * tz;
-                const uint32_t za = dz > 0 ? z0 + 1 : (z0 == 0 ? p.Z - 1 : z0 - 1);
-                const uint32_t zb = dz > 0 ? (z0 + 2 == p.Z ? 0 : z0 + 2) : z0;
-                r16[za] = (unsigned short)(w & 0xffffu);
-                r16[zb] = (unsigned short)(w >> 16);
+                const uint32_t lane = threadIdx.x & 31u;
+                if (dz > 0) {
+                    // word tz = (cell 2tz - 1, cell 2tz) after the shift
+                    const uint32_t prev = __shfl_up_sync(lanes, w, 1);
+                    if (lane > 0 && tz > 0) r[tz] = __byte_perm(prev, w, 0x5432);
+                    else r16[2 * tz + 1] = (unsigned short)(w & 0xffffu);
+                    if (lane == 31 || tz + 1 == Zh)
+                        r16[tz + 1 == Zh ? 0 : 2 * tz + 2] = (unsigned short)(w >> 16);
+                } else {
+                    // word tz = (cell 2tz + 1, cell 2tz + 2) after the shift
+                    const uint32_t next = __shfl_down_sync(lanes, w, 1);
+                    if (lane < 31 && tz + 1 < Zh) r[tz] = __byte_perm(w, next, 0x5432);
+                    else r16[2 * tz] = (unsigned short)(w >> 16);
+                    if (lane == 0 || tz == 0)
+                        r16[tz == 0 ? p.Z - 1 : 2 * tz - 1] = (unsigned short)(w & 0xffffu);
+                }
             }
         }
     }
+}
+
+// four resident blocks per SM (64 registers): occupancy hides the load latency
+// better than the registers the compiler would otherwise spend. D3Q27 (27
+// population pairs) spills 100-400 bytes at 64 registers and gets its own
+// bound.
+#ifndef LGB_VEC2_D3Q27_MIN_BLOCKS
+#define LGB_VEC2_D3Q27_MIN_BLOCKS 3
+#endif
+template <int SID, int ST, int COLL, int PAT>
+__global__ void __launch_bounds__(256, SID == LGB_D3Q27 ? LGB_VEC2_D3Q27_MIN_BLOCKS : 4)
+step_vec2_kernel(const StepParams p) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t Nh = p.N >> 1;
+    if (t >= Nh) return;
+    // lanes of this warp that hold a pair (blocks are whole warps)
+    const uint32_t base = t & ~31u;
+    const unsigned lanes = Nh - base >= 32u ? 0xffffffffu : (1u << (Nh - base)) - 1u;
+    step_pair<SID, ST, COLL, PAT>(p, t, lanes);
 }
 
 template <int SID, int ST, int COLL, int PAT>
