@@ -293,6 +293,38 @@ def _event_ms(torch, fn, steps, warmup, device):
     return start.elapsed_time(end) / steps
 
 
+def time_kbc_obstacle(lt, torch, device, peak, g, steps, warmup,
+                      strategies=("PRE_STREAMING", "POST_STREAMING")):
+    """config 3 scaled by g: D3Q27 KBC obstacle [2g, g/2, g/2], sphere of
+    diameter 24 g/256 at x = g/2 (g = 256: 512x128x128, d = 24), equilibrium
+    inlet, anti-bounce-back outlet, Re 300, u_lu 0.05, float32"""
+    import math
+    res = [2 * g, g // 2, g // 2]
+    n = int(np.prod(res))
+    flow = lt.Obstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                       res[0] / (24 * g / 256), stencil=lt.D3Q27)
+    ax = [torch.arange(k, device=device, dtype=torch.float32) for k in res]
+    X, Y, Z = torch.meshgrid(*ax, indexing="ij")
+    r = 12.0 * g / 256
+    flow.mask = ((X - g / 2) ** 2 + (Y - (res[1] - 1) / 2) ** 2 + (Z - (res[2] - 1) / 2) ** 2) < r * r
+    del X, Y, Z, ax
+    flow.initialize()
+    out = {}
+    for strat in strategies:
+        sim = lt.Simulation(flow, lt.KBCCollision(), [],
+                            streaming_strategy=getattr(lt.StreamingStrategy, strat))
+        torch.cuda.nvtx.range_push("lgb_timed")
+        ms = _event_ms(torch, sim._collide_and_stream, steps, warmup, device)
+        torch.cuda.nvtx.range_pop()
+        gbs = 217 * n / (ms * 1e-3) / 1e9
+        out[strat] = {"mlups": round(n / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms, 4),
+                      "achieved_gbs": round(gbs, 1), "frac_of_peak": round(gbs / peak, 4)}
+        del sim
+    del flow
+    torch.cuda.empty_cache()
+    return out
+
+
 def measure_configs(lt, torch, device, peak):
     """the other configurations of the workload family, each at full size
     with a short timed run (CUDA events, inputs larger than L2):
@@ -306,26 +338,8 @@ def measure_configs(lt, torch, device, peak):
     checkpoint every 20 steps."""
     import math
     out = {}
-    res = [512, 128, 128]
-    n = int(np.prod(res))
-    flow = lt.Obstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
-                       512 / 24, stencil=lt.D3Q27)
-    g = [torch.arange(k, device=device, dtype=torch.float32) for k in res]
-    X, Y, Z = torch.meshgrid(*g, indexing="ij")
-    flow.mask = ((X - 128.0) ** 2 + (Y - 63.5) ** 2 + (Z - 63.5) ** 2) < 144
-    del X, Y, Z
-    flow.initialize()
     c3 = {"workload": "D3Q27 KBC obstacle 512x128x128, float32", "bytes_per_cell": 217}
-    for strat in ("PRE_STREAMING", "POST_STREAMING"):
-        sim = lt.Simulation(flow, lt.KBCCollision(), [],
-                            streaming_strategy=getattr(lt.StreamingStrategy, strat))
-        ms = _event_ms(torch, sim._collide_and_stream, 100, 10, device)
-        gbs = 217 * n / (ms * 1e-3) / 1e9
-        c3[strat] = {"mlups": round(n / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms, 4),
-                     "achieved_gbs": round(gbs, 1), "frac_of_peak": round(gbs / peak, 4)}
-        del sim
-    del flow, g
-    torch.cuda.empty_cache()
+    c3.update(time_kbc_obstacle(lt, torch, device, peak, 256, 100, 10))
     out["config3_kbc_obstacle"] = c3
 
     c4 = {"workload": "256 D2Q9 TRT Taylor-Green domains, sides in [32, 512], Re in [100, 5000]"}
@@ -407,6 +421,30 @@ def run_ours(args, world, rank, local):
     variants = {}
     clocks = None
     wanted = set(args.variants.split(","))
+    if args.profile_only and ({"batched_f32", "batched_f16"} & wanted):
+        out = {}
+        for key, storage in [("batched_f32", None), ("batched_f16", "fp16_shifted")]:
+            if key not in wanted:
+                continue
+            flows, colls = lt.batched_taylor_green(
+                lt.Context(device, torch.float32, storage=storage), 256, seed=0)
+            sim = lt.BatchedSimulation(flows, colls)
+            torch.cuda.nvtx.range_push("lgb_timed")
+            ms = _event_ms(torch, sim.step_once, args.steps, args.warmup, device)
+            torch.cuda.nvtx.range_pop()
+            out[key] = {"cells": sim.n_cells, "ms_per_step": round(ms, 4),
+                        "mlups": round(sim.n_cells / (ms * 1e-3) / 1e6, 1)}
+            del flows, colls, sim
+            torch.cuda.empty_cache()
+        print(json.dumps({"batched": out}), flush=True)
+        return 0
+    if args.profile_only and ({"kbc_pre", "kbc_post"} & wanted):
+        strats = [s for k, s in [("kbc_pre", "PRE_STREAMING"), ("kbc_post", "POST_STREAMING")]
+                  if k in wanted]
+        print(json.dumps({"kbc_obstacle": time_kbc_obstacle(lt, torch, device, peak, args.grid,
+                                                            args.steps, args.warmup, strats),
+                          "grid": [2 * args.grid, args.grid // 2, args.grid // 2]}), flush=True)
+        return 0
     for key, storage, pattern in [("f32_pull", None, "pull"), ("f16s_pull", "fp16_shifted", "pull"),
                                   ("f32_aa", None, "aa"), ("f16s_aa", "fp16_shifted", "aa")]:
         if key not in wanted:
@@ -528,7 +566,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--grid", type=int, default=256,
                     help="cube side (profiling a smaller case; the benchmark is 256)")
-    ap.add_argument("--variants", default="f32_pull,f16s_pull,f32_aa,f16s_aa")
+    ap.add_argument("--variants", default="f32_pull,f16s_pull,f32_aa,f16s_aa",
+                    help="D3Q19 variants; with --profile-only also kbc_pre / kbc_post "
+                         "(the D3Q27 KBC obstacle [2g, g/2, g/2], g = --grid) or "
+                         "batched_f32 / batched_f16 (the 256 batched D2Q9 domains, eager "
+                         "launches)")
     ap.add_argument("--profile-only", action="store_true",
                     help="time the selected variants only and print them")
     args = ap.parse_args()
