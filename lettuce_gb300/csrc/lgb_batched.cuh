@@ -64,7 +64,6 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
             continue;
         }
         g.N = (uint32_t)n64;
-        const FastDiv divZ = FastDiv::make_device(g.Z), divY = FastDiv::make_device(g.Y);
         CollideParams cp;
         cp.omega = 1.0 / dom.tau;
         cp.inv_2tp = 1.0 / (2.0 * dom.tau);
@@ -72,26 +71,41 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
         cp.beta = 1.0 / (2.0 * dom.tau);
         const T *__restrict__ fin = pool_in + dom.offset;
         T *fout = pool_out + dom.offset;
-        const uint32_t first = (uint32_t)tile.row_begin * g.Z;
-        const uint32_t last = (uint32_t)tile.row_end * g.Z;
+        // a thread's cells advance by blockDim along the tile's rows: the
+        // row and column are carried forward (one division per tile instead
+        // of fast-division constants derived per tile)
+        const uint32_t step = blockDim.x;
         if constexpr (HSPACE) {
             if ((g.Z & 1u) == 0 && (dom.offset & 1) == 0) {
                 g.f_in = fin;
                 g.f_out = fout;
-                g.divZ = FastDiv::make_device(g.Z >> 1);
-                g.divY = divY;
                 g.cp = cp;
                 g.status = p.status;
-                for (uint32_t t2 = (first >> 1) + threadIdx.x; t2 < (last >> 1); t2 += blockDim.x)
-                    step_pair<SID, ST, COLL, LGB_PULL>(g, t2);
+                const uint32_t Zh = g.Z >> 1;
+                const uint32_t end = (uint32_t)tile.row_end * Zh;
+                uint32_t t2 = (uint32_t)tile.row_begin * Zh + threadIdx.x;
+                if (t2 >= end) continue;
+                uint32_t row = t2 / Zh, tz = t2 - row * Zh;
+                uint32_t x = row / g.Y, y = row - x * g.Y;
+                while (true) {
+                    step_pair_at<SID, ST, COLL, LGB_PULL>(g, tz, x, y);
+                    t2 += step;
+                    if (t2 >= end) break;
+                    tz += step;
+                    while (tz >= Zh) {
+                        tz -= Zh;
+                        if (++y == g.Y) { y = 0; ++x; }
+                    }
+                }
                 continue;
             }
         }
-        for (uint32_t n = first + threadIdx.x; n < last; n += blockDim.x) {
-            const uint32_t row = divZ.div(n);
-            const uint32_t z = n - row * g.Z;
-            const uint32_t x = divY.div(row);
-            const uint32_t y = row - x * g.Y;
+        const uint32_t end = (uint32_t)tile.row_end * g.Z;
+        uint32_t n = (uint32_t)tile.row_begin * g.Z + threadIdx.x;
+        if (n >= end) continue;
+        uint32_t row = n / g.Z, z = n - row * g.Z;
+        uint32_t x = row / g.Y, y = row - x * g.Y;
+        while (true) {
             Nbr c;
             c.set(x, y, z, g);
             R f[S::Q];
@@ -111,6 +125,13 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
             const size_t N = g.N;
 #pragma unroll
             for (int q = 0; q < S::Q; ++q) store_value<Sto, HSPACE>(fout + (size_t)q * N + n, f[q], S::w(q));
+            n += step;
+            if (n >= end) break;
+            z += step;
+            while (z >= g.Z) {
+                z -= g.Z;
+                if (++y == g.Y) { y = 0; ++x; }
+            }
         }
     }
 }

@@ -222,18 +222,46 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
             return -ds_val[3];
         }
     };
-    // delta_h is formed twice (for the entropy sums, then for the update)
-    // rather than kept in Q more registers
-    auto delta_h = [&](int q) -> R { return f[q] - feq_q<S>(q, rho, u, uu) - ds(q); };
-    R sum_s = R(0), sum_h = R(0);
+    // The entropic sums and the update run over opposite pairs (q, o): the
+    // equilibrium's even part w rho (1 - 1.5 u.u + 4.5 (e.u)^2) is shared,
+    // its odd part w rho 3 e.u changes sign, and delta_s is the same for
+    // both. delta_h is formed twice (for the sums, then for the update)
+    // rather than kept in Q more registers.
+    const R c0 = R(1) - R(1.5) * uu;
+    auto feq_pair = [&](int q, R &fq, R &fo) {
+        R eu = R(0);
 #pragma unroll
-    for (int q = 0; q < S::Q; ++q) {
-        const R feq = feq_q<S>(q, rho, u, uu);
+        for (int d = 0; d < S::D; ++d) {
+            const int c = S::e(q, d);
+            if (c == 1) eu += u[d];
+            else if (c == -1) eu -= u[d];
+        }
+        const R wr = R(S::w(q)) * rho;
+        const R even = wr * (c0 + R(4.5) * eu * eu);
+        const R odd = wr * (R(3) * eu);
+        fq = even + odd;
+        fo = even - odd;
+    };
+    const R feq0 = R(S::w(0)) * rho * c0;
+    R sum_s, sum_h;
+    {
+        const R d_s = ds(0);
+        const R dh = f[0] - feq0 - d_s;
+        const R ifeq = kbc_rcp(feq0);
+        sum_s = d_s * dh * ifeq;
+        sum_h = dh * dh * ifeq;
+    }
+#pragma unroll
+    for (int q = 1; q < S::Q; ++q) {
+        const int o = S::opp(q);
+        if (o < q) continue;
+        R fq, fo;
+        feq_pair(q, fq, fo);
         const R d_s = ds(q);
-        const R dh = f[q] - feq - d_s;
-        const R ifeq = kbc_rcp(feq);
-        sum_s += d_s * dh * ifeq;
-        sum_h += dh * dh * ifeq;
+        const R hq = f[q] - fq - d_s, ho = f[o] - fo - d_s;
+        const R iq = kbc_rcp(fq), io = kbc_rcp(fo);
+        sum_s += d_s * (hq * iq + ho * io);
+        sum_h += hq * hq * iq + ho * ho * io;
     }
     const R beta = R(cp.beta);
     const R ib = R(1) / beta;
@@ -241,10 +269,20 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     // kbc_collision.py:155-158: gamma < 1e-15 or NaN -> 2
     if (!(gamma >= R(1e-15))) gamma = R(2);
     const R b2 = R(2) * beta, bg = beta * gamma;
+    {
+        const R d_s = ds(0);
+        f[0] = f[0] - b2 * d_s - bg * (f[0] - feq0 - d_s);
+    }
 #pragma unroll
-    for (int q = 0; q < S::Q; ++q) {
-        const R dh = delta_h(q);
-        f[q] = f[q] - b2 * ds(q) - bg * dh;
+    for (int q = 1; q < S::Q; ++q) {
+        const int o = S::opp(q);
+        if (o < q) continue;
+        R fq, fo;
+        feq_pair(q, fq, fo);
+        const R d_s = ds(q);
+        const R hq = f[q] - fq - d_s, ho = f[o] - fo - d_s;
+        f[q] = f[q] - b2 * d_s - bg * hq;
+        f[o] = f[o] - b2 * d_s - bg * ho;
     }
     rho_out = rho;
 }

@@ -34,15 +34,6 @@ struct FastDiv {
         f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
         return f;
     }
-    // the same magic numbers computed on the device (per tile of a batch)
-    __device__ __forceinline__ static FastDiv make_device(uint32_t d) {
-        FastDiv f;
-        f.d = d;
-        const uint32_t l = d <= 1 ? 0u : 32u - __clz(d - 1);
-        f.s = l;
-        f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
-        return f;
-    }
     __device__ __forceinline__ uint32_t div(uint32_t n) const {
         if (s == 0) return n;
         const uint32_t t = __umulhi(m, n);
@@ -425,7 +416,9 @@ StepTables<SID, ST, COLL> make_tables(const StepParams &p) {
 
 template <int SID, int ST, int COLL, int PAT, int MASK>
 cudaError_t launch_step(const StepParams &p, cudaStream_t stream) {
-    const unsigned threads = 256;
+    // the outlet plane has few cells (128 x 128 for the obstacle): smaller
+    // blocks spread them over more SMs
+    const unsigned threads = MASK == 2 ? 64 : 256;
     uint64_t count = p.N;
     if (MASK == 2) {
         const uint32_t ax = p.abb_axis == 0 ? p.X : (p.abb_axis == 1 ? p.Y : p.Z);

@@ -48,20 +48,18 @@ __device__ __forceinline__ uint32_t load_pair(const uint32_t *__restrict__ row, 
     return __byte_perm(__ldg(row + tz), __ldg(row + tzp), 0x5432);
 }
 
-// the step of cell pair t (cells 2t, 2t + 1 of the grid p, t < N / 2);
-// p.divZ holds Z / 2. For PUSH and AA_ODD, pair t must be held by lane
+// the step of the cell pair tz (cells 2 tz, 2 tz + 1) of row (x, y) of the
+// grid p. For PUSH and AA_ODD, pair t = row Z/2 + tz must be held by lane
 // t mod 32 of a warp whose active lanes are `lanes`.
 template <int SID, int ST, int COLL, int PAT>
-__device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
-                                          const unsigned lanes = 0xffffffffu) {
+__device__ __forceinline__ void step_pair_at(const StepParams &p, const uint32_t tz,
+                                             const uint32_t x, const uint32_t y,
+                                             const unsigned lanes = 0xffffffffu) {
     using S = Stencil<SID>;
     using P = Pack16<ST>;
     const uint32_t Zh = p.Z >> 1;
     const uint32_t Nh = p.N >> 1;
-    const uint32_t row = p.divZ.div(t);
-    const uint32_t tz = t - row * Zh;
-    const uint32_t x = p.divY.div(row);
-    const uint32_t y = row - x * p.Y;
+    const uint32_t row = x * p.Y + y;
     const uint32_t xm = x == 0 ? p.X - 1 : x - 1, xp = x + 1 == p.X ? 0 : x + 1;
     const uint32_t ym = y == 0 ? p.Y - 1 : y - 1, yp = y + 1 == p.Y ? 0 : y + 1;
     const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
@@ -134,6 +132,14 @@ __device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
             }
         }
     }
+}
+
+template <int SID, int ST, int COLL, int PAT>
+__device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
+                                          const unsigned lanes = 0xffffffffu) {
+    const uint32_t row = p.divZ.div(t);
+    const uint32_t x = p.divY.div(row);
+    step_pair_at<SID, ST, COLL, PAT>(p, t - row * (p.Z >> 1), x, row - x * p.Y, lanes);
 }
 
 // four resident blocks per SM (64 registers): occupancy hides the load latency

@@ -90,11 +90,14 @@ def test_adjoint_kernel_equals_torch_vjp(lgb, S, res):
 
 
 def test_checkpoint_interval_does_not_change_gradient(lgb):
+    """k = 1 runs eagerly, 7 (odd: both field parities, a 2-step remainder)
+    and 20 replay captured segments, 1000 is one segment; repeated k replay
+    the graphs kept in the workspace"""
     gen = torch.Generator().manual_seed(2)
     u0 = (0.02 * torch.randn(2, 40, 36, generator=gen)).cuda()
     target = (0.02 * torch.randn(2, 40, 36, generator=gen)).cuda()
     grads = []
-    for k in (1, 7, 20, 1000):
+    for k in (1, 7, 7, 20, 20, 1000):
         x = u0.clone().requires_grad_(True)
         _loss(x, target, 0.57, 30, torch.float32, k=k).backward()
         grads.append(x.grad.clone())
