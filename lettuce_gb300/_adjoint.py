@@ -99,10 +99,7 @@ class _Workspace:
     def _graph(self, table, key, fn):
         g = table.get(key)
         if g is None:
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.device(self.device), \
-                    torch.cuda.graph(g, capture_error_mode="thread_local"):
-                fn(torch.cuda.current_stream(self.device).cuda_stream)
+            g = _device.capture(self.device, fn)
             table[key] = g
         return g
 

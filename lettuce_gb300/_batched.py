@@ -185,18 +185,17 @@ class BatchedSimulation:
 
     def _capture(self):
         """a CUDA graph of two steps: pool 0 -> 1 -> 0"""
-        g = torch.cuda.CUDAGraph()
         s = torch.cuda.Stream(self.context.device)
         s.wait_stream(torch.cuda.current_stream(self.context.device))
         with torch.cuda.stream(s):
             self._launch(self._pools[0], self._pools[1], s.cuda_stream)  # warm outside capture
             self._launch(self._pools[1], self._pools[0], s.cuda_stream)
         torch.cuda.current_stream(self.context.device).wait_stream(s)
-        with torch.cuda.graph(g):
-            st = torch.cuda.current_stream(self.context.device).cuda_stream
+
+        def pair(st):
             self._launch(self._pools[0], self._pools[1], st)
             self._launch(self._pools[1], self._pools[0], st)
-        self._graph = g
+        self._graph = _device.capture(self.context.device, pair)
         self._graph_key = (self.threads, self.tile_cells)
 
     def advance(self, num_steps: int, use_graph: bool = True):

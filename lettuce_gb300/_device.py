@@ -130,3 +130,24 @@ def bcast_strides(t: torch.Tensor, full_shape: Sequence[int]) -> list:
 
 def as_numpy_f64(t: torch.Tensor) -> np.ndarray:
     return t.detach().to(torch.float64).cpu().numpy()
+
+
+def capture(device: torch.device, launch) -> "torch.cuda.CUDAGraph":
+    """A CUDA graph of the launches ``launch(stream_handle)`` makes, captured
+    on a side stream ordered after the current one. Unlike the
+    ``torch.cuda.graph`` context manager this neither synchronises the
+    device nor empties torch's allocator cache nor runs the garbage
+    collector, so a re-capture (new field pointers) costs about as much as
+    the launches themselves. The launches must not allocate memory."""
+    g = torch.cuda.CUDAGraph()
+    cur = torch.cuda.current_stream(device)
+    side = torch.cuda.Stream(device)
+    side.wait_stream(cur)
+    with torch.cuda.device(device), torch.cuda.stream(side):
+        g.capture_begin(capture_error_mode="thread_local")
+        try:
+            launch(side.cuda_stream)
+        finally:
+            g.capture_end()
+    cur.wait_stream(side)
+    return g

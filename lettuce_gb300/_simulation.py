@@ -284,10 +284,11 @@ class Simulation:
         if self.context.device.type != "cuda":
             raise RuntimeError("lettuce_gb300 steps on CUDA devices only; there is no CPU path")
 
-    def _collide_and_stream(self, *_, **__):
+    def _collide_and_stream(self, *_, stream=None, **__):
         flow = self.flow
         d = self._desc
-        stream = self.context.stream_handle()
+        if stream is None:
+            stream = self.context.stream_handle()
         if self.memory_pattern == "aa":
             d.pattern = _lib.AA_ODD if flow._aa_pending else _lib.AA_EVEN
             d.f_in = d.f_out = flow._f.data_ptr()
@@ -338,10 +339,10 @@ class Simulation:
                 self._collide_and_stream(self)
                 flow.i += 1
             n -= 2
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                self._collide_and_stream(self)
-                self._collide_and_stream(self)
+            def pair(stream):
+                self._collide_and_stream(self, stream=stream)
+                self._collide_and_stream(self, stream=stream)
+            g = _device.capture(self.context.device, pair)
             if len(self._graph) >= 4:
                 self._graph.clear()
             self._graph[self._state_key()] = g

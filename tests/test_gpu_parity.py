@@ -137,6 +137,14 @@ ORACLE_CASES = [
     ("D1Q3", [129], "bgk", "PRE_STREAMING", 50),
     ("D2Q9", [30, 20], "bgk", "DOUBLE_STREAMING", 20),
     ("D3Q19", [8, 9, 10], "bgk", "NO_STREAMING", 10),
+    # degenerate extents: a dimension of one or two cells wraps onto itself
+    ("D3Q19", [1, 5, 7], "bgk", "PRE_STREAMING", 6),
+    ("D3Q19", [4, 1, 2], "trt", "POST_STREAMING", 6),
+    ("D3Q27", [2, 3, 1], "kbc", "PRE_STREAMING", 4),
+    ("D2Q9", [1, 1], "bgk", "POST_STREAMING", 5),
+    ("D2Q9", [2, 3], "trt", "PRE_STREAMING", 5),
+    ("D1Q3", [1], "bgk", "PRE_STREAMING", 5),
+    ("D1Q3", [2], "trt", "POST_STREAMING", 5),
 ]
 
 
@@ -288,6 +296,28 @@ def test_two_cell_kernel_bit_identical(lgb, storage, S, res, coll, pattern):
         sim(7)
         out.append(flow.f.clone())
     assert torch.equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("res", [[3, 1, 2], [1, 1, 2], [2, 2, 2]])
+@pytest.mark.parametrize("pattern", ["pull", "push", "aa"])
+def test_two_cell_kernel_tiny_rows(lgb, res, pattern):
+    """rows of two cells (one pair per row: the shifted pair wraps onto
+    itself) give the same populations in the two-cell and one-cell kernels"""
+    from lettuce_gb300 import _lib
+    f0 = _tgv_like("D3Q19", res, 5)
+    outs = []
+    for one_cell in (False, True):
+        c = lt.Context("cuda:0", F32, storage="fp16_shifted")
+        flow = GivenFlow(c, lt.D3Q19(), f0)
+        kw = ({"memory_pattern": "aa"} if pattern == "aa" else
+              {"streaming_strategy": STRATS["PRE_STREAMING" if pattern == "pull"
+                                            else "POST_STREAMING"]})
+        sim = lt.Simulation(flow, lt.BGKCollision(0.6), [], use_graph=False, **kw)
+        if one_cell:
+            sim._desc.options |= _lib.OPT_ONE_CELL
+        sim(5)
+        outs.append(flow.f_raw.clone())
+    assert torch.equal(outs[0], outs[1])
 
 
 def test_shifted_storage_matches_f32_closely(lgb, oracle):
