@@ -268,6 +268,20 @@ int lgb_adjoint_step(int32_t stencil, int32_t storage, const int32_t *res, doubl
 int lgb_convert(int32_t stencil, int32_t src_storage, const void *src,
                 int32_t dst_storage, void *dst, int64_t n_cells, void *stream);
 
+/* The device address of page-locked, mapped host memory (memory from
+ * cudaHostAlloc / cudaMallocHost, or registered with cudaHostRegister and
+ * the mapped flag); fails for host memory the device cannot address (on a
+ * host whose GPU reads pageable memory through the host page tables, such
+ * as a Grace host, pageable memory is addressable too). With that address
+ * lgb_convert moves a population field between host and device memory in
+ * one kernel over the host link, converting the storage format on the way.
+ * No lettuce counterpart: lettuce moves fields with torch copies
+ * (lettuce/_flow.py:258-268, Context.convert_to_tensor). A kernel is used
+ * because on a GB300 host the copy engines' first device-to-host transfer
+ * after a period of GPU work runs at a tenth of the link rate, while kernel
+ * stores to mapped host memory do not. */
+int lgb_host_pointer(const void *host, void **device);
+
 #ifdef __cplusplus
 }
 #endif

@@ -96,6 +96,28 @@ def convert(stencil_id: int, src: torch.Tensor, src_storage: int, dst: torch.Ten
                              dst.data_ptr(), int(n_cells), stream_of(src)), "lgb_convert")
 
 
+def host_device_pointer(t: torch.Tensor) -> Optional[int]:
+    """The device address of a page-locked host tensor's data, or None when
+    ``t`` is not in page-locked, mapped host memory."""
+    if t.device.type != "cpu" or not t.is_pinned():
+        return None
+    L = _lib.load()
+    base = t.untyped_storage().data_ptr()
+    out = ctypes.c_void_p()
+    if L.lgb_host_pointer(ctypes.c_void_p(base), ctypes.byref(out)) != 0 or not out.value:
+        return None
+    return out.value + (t.data_ptr() - base)
+
+
+def convert_ptr(stencil_id: int, src_ptr: int, src_storage: int, dst_ptr: int, dst_storage: int,
+                n_cells: int, stream: int):
+    """lgb_convert on raw addresses (device memory, or host memory through
+    host_device_pointer)"""
+    L = _lib.load()
+    _lib.check(L.lgb_convert(stencil_id, src_storage, ctypes.c_void_p(src_ptr), dst_storage,
+                             ctypes.c_void_p(dst_ptr), int(n_cells), stream), "lgb_convert")
+
+
 def step(desc: _lib.StepDesc, stream: int):
     L = _lib.load()
     _lib.check(L.lgb_step(ctypes.byref(desc), stream), "lgb_step")

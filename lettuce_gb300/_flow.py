@@ -154,6 +154,8 @@ class Flow(ABC):
     def f(self, value: torch.Tensor):
         value = torch.as_tensor(value)
         self._aa_pending = False
+        if self._upload_pinned(value):
+            return
         if self.context.shifted:
             v = value.to(device=self.context.device, dtype=torch.float32)
             self._f = (v - _weights_view(self, torch.float32)).to(
@@ -162,6 +164,51 @@ class Flow(ABC):
             if value.dtype != self.context.dtype or value.device != self.context.device:
                 value = value.to(device=self.context.device, dtype=self.context.dtype)
             self._f = value if value.is_contiguous() else value.contiguous()
+
+    # -- host transfers ----------------------------------------------------
+    def _host_transfer_ok(self, t: torch.Tensor) -> bool:
+        return (self.context.device.type == "cuda" and t.device.type == "cpu"
+                and t.dtype == self.context.dtype and t.is_contiguous()
+                and list(t.shape) == [self.stencil.q] + list(self.resolution))
+
+    def _upload_pinned(self, value: torch.Tensor) -> bool:
+        """a page-locked host field in the context dtype goes to the device
+        through one conversion kernel reading host memory (storage format
+        applied on the way); False when that path does not apply"""
+        if not self._host_transfer_ok(value):
+            return False
+        ptr = _device.host_device_pointer(value)
+        if ptr is None:
+            return False
+        out = torch.empty([self.stencil.q] + list(self.resolution),
+                          dtype=self.context.storage_dtype, device=self.context.device)
+        _device.convert_ptr(self.stencil.lgb_id, ptr, _device.storage_of(value.dtype),
+                            out.data_ptr(), self.context.storage, out[0].numel(),
+                            torch.cuda.current_stream(self.context.device).cuda_stream)
+        self._f = out
+        return True
+
+    def download(self, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """The populations in the context dtype, written into ``out`` (a host
+        tensor; allocated page-locked when None). Into page-locked host memory
+        one conversion kernel writes them over the host link, asynchronously
+        on the current stream (synchronise before reading ``out``); any other
+        ``out`` takes a torch copy."""
+        shape = [self.stencil.q] + list(self.resolution)
+        if out is None:
+            out = torch.empty(shape, dtype=self.context.dtype,
+                              pin_memory=self.context.device.type == "cuda")
+        if self._host_transfer_ok(out):
+            ptr = _device.host_device_pointer(out)
+            if ptr is not None:
+                if self._aa_pending:
+                    self._unpack_aa()
+                _device.convert_ptr(self.stencil.lgb_id, self._f.data_ptr(), self.context.storage,
+                                    ptr, _device.storage_of(out.dtype), out[0].numel(),
+                                    torch.cuda.current_stream(self.context.device).cuda_stream)
+                return out
+        out.copy_(self.f, non_blocking=True)
+        return out
 
     @property
     def f_raw(self) -> torch.Tensor:

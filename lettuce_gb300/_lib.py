@@ -30,7 +30,7 @@ OPT_ONE_CELL, OPT_PUSH_GUARD = 1, 2
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
             "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_reduce_static", "lgb_convert",
-            "lgb_batch_plan", "lgb_batched_step", "lgb_adjoint_step"]
+            "lgb_batch_plan", "lgb_batched_step", "lgb_adjoint_step", "lgb_host_pointer"]
 REDUCE_STATIC_SCRATCH_BYTES = 48640
 
 
@@ -114,6 +114,8 @@ def load():
         L.lgb_adjoint_step.argtypes = [I32, I32, P, ctypes.c_double, P, P, P, P]
         L.lgb_adjoint_step.restype = ctypes.c_int
         L.lgb_convert.restype = ctypes.c_int
+        L.lgb_host_pointer.argtypes = [P, ctypes.POINTER(ctypes.c_void_p)]
+        L.lgb_host_pointer.restype = ctypes.c_int
         if L.lgb_abi_version() != ABI_VERSION:
             raise LibraryError(f"{path} has ABI version {L.lgb_abi_version()}, "
                                f"expected {ABI_VERSION}; rebuild it")

@@ -650,6 +650,19 @@ int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res, cons
     return 0;
 }
 
+int lgb_host_pointer(const void *host, void **device) {
+    if (!host || !device) return fail("lgb_host_pointer: NULL pointer");
+    void *d = nullptr;
+    const cudaError_t e = cudaHostGetDevicePointer(&d, const_cast<void *>(host), 0);
+    if (e != cudaSuccess || !d) {
+        cudaGetLastError();  // not sticky; leave no error behind for the next call
+        return fail("lgb_host_pointer: not page-locked, mapped host memory (%s)",
+                    cudaGetErrorString(e));
+    }
+    *device = d;
+    return 0;
+}
+
 int lgb_convert(int32_t stencil, int32_t src_storage, const void *src, int32_t dst_storage,
                 void *dst, int64_t n_cells, void *stream) {
     int dd, q;

@@ -1,0 +1,59 @@
+"""Properties at the benchmark's full size (D3Q19 Taylor-Green 256^3), where
+the oracle is too slow to run: total mass and momentum are conserved by
+the periodic step (float64 sums of the device reductions and moments), the
+in-place AA pattern equals the push pattern bit for bit, and the two-cell
+16-bit kernel equals the one-cell kernel bit for bit."""
+import pytest
+import torch
+
+import lettuce_gb300 as lt
+from lettuce_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+RES = [256, 256, 256]
+
+
+def tgv(dtype=torch.float32, storage=None):
+    return lt.TaylorGreenVortex(lt.Context("cuda:0", dtype, storage=storage), RES, 1600, 0.05,
+                                lt.D3Q19)
+
+
+def totals(flow):
+    rho = flow.rho().double()
+    j = flow.j().double()
+    return rho.sum().item(), j.sum(dim=tuple(range(1, j.dim()))), j.abs().sum().item()
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-13), (torch.float32, 2e-6)])
+def test_mass_and_momentum_conserved(lgb, dtype, tol):
+    flow = tgv(dtype)
+    m0, j0, jabs = totals(flow)
+    lt.Simulation(flow, lt.BGKCollision(flow.units.relaxation_parameter_lu), [],
+                  streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)(100)
+    m1, j1, _ = totals(flow)
+    assert abs(m1 / m0 - 1) < tol
+    assert torch.max(torch.abs(j1 - j0)).item() / jabs < tol
+
+
+@pytest.mark.parametrize("storage", [None, "fp16_shifted"])
+def test_aa_equals_push_full_size(lgb, storage):
+    a, b = tgv(storage=storage), tgv(storage=storage)
+    tau = a.units.relaxation_parameter_lu
+    lt.Simulation(a, lt.BGKCollision(tau), [], memory_pattern="aa")(8)
+    lt.Simulation(b, lt.BGKCollision(tau), [],
+                  streaming_strategy=lt.StreamingStrategy.POST_STREAMING)(8)
+    assert torch.equal(a.f, b.f)
+
+
+def test_two_cell_equals_one_cell_full_size(lgb):
+    a, b = tgv(storage="fp16_shifted"), tgv(storage="fp16_shifted")
+    tau = a.units.relaxation_parameter_lu
+    sa = lt.Simulation(a, lt.BGKCollision(tau), [],
+                       streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+    sb = lt.Simulation(b, lt.BGKCollision(tau), [],
+                       streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+    sb._desc.options |= _lib.OPT_ONE_CELL
+    sa(6)
+    sb(6)
+    assert torch.equal(a.f_raw, b.f_raw)
