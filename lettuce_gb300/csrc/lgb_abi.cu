@@ -478,6 +478,7 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
         if (p.has_nsm && (d->pattern == LGB_AA_EVEN || d->pattern == LGB_AA_ODD))
             return fail("lgb_step: no-streaming masks are not supported by the AA pattern");
         p.n_sub = d->n_sub;
+        p.coll_idx = d->collision_index;
         const int off = 3 - g.d;
         for (int k = 0; k < d->n_sub; ++k) {
             const lgb_substep &s = d->sub[k];

@@ -65,6 +65,7 @@ struct StepParams {
     int32_t has_nsm;
     int32_t push_guard;  // the flags carry LGB_FLAG_PUSH_GUARD
     int32_t n_sub;
+    int32_t coll_idx;    // substep index of the collision
     // the anti-bounce-back outlet (at most one): its substep index (-1 for
     // none), internal axis of its normal (0=X, 1=Y, 2=Z), sign, plane and
     // neighbour-plane coordinates along that axis
@@ -111,18 +112,25 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
                                           const Nbr &c, uint32_t n, uint32_t nsbits,
                                           typename Sto::R (&f)[S::Q]) {
     const size_t N = p.N;
+    // a pull with no-streaming bits keeps the cell's own value for those
+    // populations; cells without any (nearly all) skip the per-population test
+    const bool keep_own = MASKED && LOAD == LOAD_PULL && nsbits != 0;
+    auto load_all = [&](const bool check) {
 #pragma unroll
-    for (int q = 0; q < S::Q; ++q) {
-        uint32_t src = n;
-        int slot = q;
-        if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
-            src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
-            if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
-            if (MASKED && LOAD == LOAD_PULL && q != 0 && ((nsbits >> q) & 1u)) src = n;
+        for (int q = 0; q < S::Q; ++q) {
+            uint32_t src = n;
+            int slot = q;
+            if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
+                src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
+                if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
+                if (check && q != 0 && ((nsbits >> q) & 1u)) src = n;
+            }
+            if constexpr (RAW) f[q] = Sto::load_h(fin + (size_t)slot * N + src);
+            else f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
         }
-        if constexpr (RAW) f[q] = Sto::load_h(fin + (size_t)slot * N + src);
-        else f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
-    }
+    };
+    if (keep_own) load_all(true);
+    else load_all(false);
 }
 
 // the substep with index `idx`, copied out of the parameter block by an
@@ -155,10 +163,10 @@ __device__ __forceinline__ SubParams select_sub(const StepParams &p, int idx) {
 }
 
 // substep `sb` (collision, bounce-back, equilibrium BC or none) at one cell
-template <class S, int COLL, class R, class TT>
+template <class S, int COLL, bool WITH_COLLISION = true, class R, class TT>
 __device__ __forceinline__ void apply_local_substep(const StepParams &p, const SubParams &sb,
                                                     const Nbr &c, R (&f)[S::Q], const TT &tab) {
-    if (sb.kind == LGB_SUB_COLLISION) {
+    if (WITH_COLLISION && sb.kind == LGB_SUB_COLLISION) {
         R r;
         collide<COLL, S>(f, p.cp, r, tab);
     } else if (sb.kind == LGB_SUB_BOUNCE_BACK) {
@@ -314,8 +322,15 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
             collide_shifted<S, Lane1, COLL>(f, p.cp);
     } else if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
         if constexpr (MASK == 1) {
-            // a cell off the outlet plane runs the substep its index names
-            apply_local_substep<S, COLL>(p, select_sub(p, fl & LGB_FLAG_INDEX_MASK), c, f, tab);
+            // a cell off the outlet plane runs the substep its index names;
+            // the collision (most cells) without copying out a substep record
+            const int idx = fl & LGB_FLAG_INDEX_MASK;
+            if (idx == p.coll_idx) {
+                R r;
+                collide<COLL, S>(f, p.cp, r, tab);
+            } else {
+                apply_local_substep<S, COLL, false>(p, select_sub(p, idx), c, f, tab);
+            }
         } else if constexpr (MASK == 2) {
             // an outlet-plane cell runs the substep its index names and the
             // outlet substep, in sequence order
