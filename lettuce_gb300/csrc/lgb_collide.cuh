@@ -134,6 +134,51 @@ LGB_HD float kbc_rcp(float x) {
 }
 LGB_HD double kbc_rcp(double x) { return 1.0 / x; }
 
+// the population index of velocity (x, y, z) of a 3-D stencil
+template <class S> LGB_HD constexpr int q_of(int x, int y, int z) {
+    for (int q = 0; q < S::Q; ++q)
+        if (S::e(q, 0) == x && S::e(q, 1) == y && S::e(q, 2) == z) return q;
+    return -1;
+}
+
+// D3Q27: density, momentum and the second moments m_ab = sum_q e_qa e_qb f_q
+// (packed xx, yy, zz, xy, xz, yz) from partial sums along the nine z-lines
+// (about 70 additions instead of about 180 for the ten sums taken one by one)
+template <class S, class R>
+LGB_HD void moments27(const R (&f)[S::Q], R &rho, R (&j)[3], R (&m)[6]) {
+    static_assert(S::Q == 27, "D3Q27 only");
+    R A[3][3], B[3][3], C[3][3];  // per (x, y) line: sum f, sum z f, sum z^2 f
+#pragma unroll
+    for (int x = -1; x <= 1; ++x) {
+#pragma unroll
+        for (int y = -1; y <= 1; ++y) {
+            const R lo = f[q_of<S>(x, y, -1)], mid = f[q_of<S>(x, y, 0)], hi = f[q_of<S>(x, y, 1)];
+            C[x + 1][y + 1] = hi + lo;
+            B[x + 1][y + 1] = hi - lo;
+            A[x + 1][y + 1] = C[x + 1][y + 1] + mid;
+        }
+    }
+    R Ax[3], Bx[3];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        Ax[x] = A[x][0] + A[x][1] + A[x][2];
+        Bx[x] = B[x][0] + B[x][1] + B[x][2];
+    }
+    const R Ayp = A[0][2] + A[1][2] + A[2][2], Aym = A[0][0] + A[1][0] + A[2][0];
+    const R Byp = B[0][2] + B[1][2] + B[2][2], Bym = B[0][0] + B[1][0] + B[2][0];
+    rho = Ax[0] + Ax[1] + Ax[2];
+    j[0] = Ax[2] - Ax[0];
+    j[1] = Ayp - Aym;
+    j[2] = Bx[0] + Bx[1] + Bx[2];
+    m[0] = Ax[2] + Ax[0];
+    m[1] = Ayp + Aym;
+    m[2] = (C[0][0] + C[0][1] + C[0][2]) + (C[1][0] + C[1][1] + C[1][2]) +
+           (C[2][0] + C[2][1] + C[2][2]);
+    m[3] = (A[2][2] - A[2][0]) - (A[0][2] - A[0][0]);
+    m[4] = Bx[2] - Bx[0];
+    m[5] = Byp - Bym;
+}
+
 // Entropic KBC collision (lettuce/ext/_collision/kbc_collision.py:96-160),
 // D3Q27 and D2Q9. The shear part delta_s = s(f) - s(feq) is linear in the
 // second moments, s(.) of kbc_collision.py:44-94; for the quadratic
@@ -147,24 +192,23 @@ template <class S, class R>
 LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     static_assert(S::Q == 27 || S::Q == 9, "KBC is defined for D3Q27 and D2Q9");
     R rho, u[3];
-    cell_moments<S>(f, rho, u);
+    R m27[6];
+    if constexpr (S::Q == 27) {
+        moments27<S>(f, rho, u, m27);
+        const R inv = R(1) / rho;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] *= inv;
+    } else {
+        cell_moments<S>(f, rho, u);
+    }
     const R uu = dot_uu<S>(u);
     const R inv_rho = R(1) / rho;
     const R third = R(1.0 / 3.0);
     // delta_s by velocity class (index into ds_val below)
     R ds_val[8];
     if constexpr (S::Q == 27) {
-        R mxx = 0, myy = 0, mzz = 0, mxy = 0, mxz = 0, myz = 0;
-#pragma unroll
-        for (int q = 0; q < 27; ++q) {
-            const int ex = S::e(q, 0), ey = S::e(q, 1), ez = S::e(q, 2);
-            if (ex) mxx += f[q];
-            if (ey) myy += f[q];
-            if (ez) mzz += f[q];
-            if (ex * ey == 1) mxy += f[q]; else if (ex * ey == -1) mxy -= f[q];
-            if (ex * ez == 1) mxz += f[q]; else if (ex * ez == -1) mxz -= f[q];
-            if (ey * ez == 1) myz += f[q]; else if (ey * ez == -1) myz -= f[q];
-        }
+        const R mxx = m27[0], myy = m27[1], mzz = m27[2], mxy = m27[3], mxz = m27[4],
+                myz = m27[5];
         const R dxx = mxx * inv_rho - (third + u[0] * u[0]);
         const R dyy = myy * inv_rho - (third + u[1] * u[1]);
         const R dzz = mzz * inv_rho - (third + u[2] * u[2]);

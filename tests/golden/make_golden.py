@@ -428,6 +428,16 @@ def case_mrt(name, stencil, transform, res, steps, seed):
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
 
 
+def case_dump():
+    """lettuce's own checkpoint file (Flow.dump, lettuce/_flow.py:258-260) of a
+    D2Q9 Taylor-Green field, written by lettuce"""
+    flow = TaylorGreenVortex(CTX, resolution=12, reynolds_number=100, mach_number=0.05,
+                             stencil=D2Q9)
+    flow.dump(os.path.join(OUT, "lettuce_dump_d2q9_12.pkl"))
+    np.savez_compressed(os.path.join(OUT, "lettuce_dump_d2q9_12.npz"), f=npf(flow.f),
+                        meta=json.dumps({"res": [12, 12], "re": 100, "ma": 0.05}))
+
+
 def main():
     torch.set_num_threads(os.cpu_count() or 1)
     case_tgv("tgv2d_d2q9_bgk", D2Q9, 16, 1000, "bgk", 5)
@@ -464,6 +474,7 @@ def main():
     case_mrt("mrt_d3q27_hermite", D3Q27, D3Q27Hermite, [4, 4, 3], 3, 72)
     case_poiseuille("poiseuille_guo", "guo", 300)
     case_poiseuille("poiseuille_shanchen", "shan_chen", 300)
+    case_dump()
     case_native_kats()
     case_observables()
     case_adjoint()

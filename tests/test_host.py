@@ -220,3 +220,20 @@ def test_checkpoint_round_trip(tmp_path):
     flow.f = torch.zeros_like(f0)
     flow.load(tmp_path / "f.pkl")
     assert torch.equal(flow.f, f0)
+
+
+def test_checkpoint_compatible_with_lettuce(tmp_path):
+    """a file written by lettuce's Flow.dump loads here, and this package's
+    dump writes the same array lettuce's load expects (a pickled ndarray)"""
+    import os
+    import pickle
+    from conftest import GOLDEN
+    ref = np.load(os.path.join(GOLDEN, "lettuce_dump_d2q9_12.npz"))["f"]
+    flow = lt.TaylorGreenVortex(CPU64, 12, 100, 0.05, lt.D2Q9)
+    flow.f = torch.zeros_like(flow.f)
+    flow.load(os.path.join(GOLDEN, "lettuce_dump_d2q9_12.pkl"))
+    assert np.array_equal(flow.f.numpy(), ref)
+    flow.dump(tmp_path / "ours.pkl")
+    with open(tmp_path / "ours.pkl", "rb") as fh:
+        back = pickle.load(fh)
+    assert isinstance(back, np.ndarray) and np.array_equal(back, ref)
