@@ -304,6 +304,31 @@ class Simulation:
             _device.step(d, stream)
             flow._f, flow._f_next = dst, src
 
+    # -- the two halves of a step (lettuce/_simulation.py:245-305) ----------
+    def _run_pattern(self, pattern: int) -> torch.Tensor:
+        self._require_device()
+        flow = self.flow
+        if flow._aa_pending:
+            flow._unpack_aa()
+        d = self._desc
+        d.pattern = pattern
+        src, dst = flow._f, flow.f_next
+        d.f_in = src.data_ptr()
+        d.f_out = dst.data_ptr()
+        _device.step(d, self.context.stream_handle())
+        flow._f, flow._f_next = dst, src
+        return flow.f
+
+    def _stream(self) -> torch.Tensor:
+        """lettuce's streaming half alone: f[q](x) <- f[q](x - e_q), keeping
+        the populations the no-streaming mask holds (one STREAM_ONLY launch)"""
+        return self._run_pattern(_lib.STREAM_ONLY)
+
+    def _collide(self) -> torch.Tensor:
+        """lettuce's collide half alone: the masked sequence of
+        pre-boundaries, collision and post-boundaries (one LOCAL launch)"""
+        return self._run_pattern(_lib.LOCAL)
+
     # -- CUDA-graph replay -------------------------------------------------
     def _graphs_enabled(self) -> bool:
         if self.use_graph is None:

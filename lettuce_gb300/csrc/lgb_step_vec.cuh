@@ -149,8 +149,11 @@ __device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
 #ifndef LGB_VEC2_D3Q27_MIN_BLOCKS
 #define LGB_VEC2_D3Q27_MIN_BLOCKS 3
 #endif
+#ifndef LGB_VEC2_MIN_BLOCKS
+#define LGB_VEC2_MIN_BLOCKS 4
+#endif
 template <int SID, int ST, int COLL, int PAT>
-__global__ void __launch_bounds__(256, SID == LGB_D3Q27 ? LGB_VEC2_D3Q27_MIN_BLOCKS : 4)
+__global__ void __launch_bounds__(256, SID == LGB_D3Q27 ? LGB_VEC2_D3Q27_MIN_BLOCKS : LGB_VEC2_MIN_BLOCKS)
 step_vec2_kernel(const StepParams p) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Nh = p.N >> 1;
