@@ -387,8 +387,9 @@ class Simulation:
             best = k if best is None else min(best, k)
         return best if best is not None else 1 << 62
 
-    def _run(self, target_done):
-        """advance until target_done() holds, reporting like lettuce"""
+    def _run(self, target_done, remaining):
+        """advance until target_done() holds, reporting like lettuce;
+        remaining() bounds the steps taken before the next check"""
         graphs = self._graphs_enabled()
         while not target_done():
             if not graphs:
@@ -396,7 +397,7 @@ class Simulation:
                 self.flow.i += 1
                 self._report()
                 continue
-            m = min(self._steps_to_next_report(), self._remaining())
+            m = min(self._steps_to_next_report(), remaining())
             self._advance(m)
             self._report()
 
@@ -415,8 +416,7 @@ class Simulation:
         if self.flow.i == 0:
             self._report()
         stop = self.flow.i + num_steps
-        self._remaining = lambda: stop - self.flow.i
-        self._run(lambda: self.flow.i >= stop)
+        self._run(lambda: self.flow.i >= stop, lambda: stop - self.flow.i)
         self.context.synchronize()
         end = timer()
         return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)
@@ -434,8 +434,7 @@ class BreakableSimulation(Simulation):
         beg = timer()
         if self.flow.i == 0:
             self._report()
-        self._remaining = lambda: max(1, num_steps - self.flow.i)
-        self._run(lambda: self.flow.i >= num_steps)
+        self._run(lambda: self.flow.i >= num_steps, lambda: max(1, num_steps - self.flow.i))
         self.context.synchronize()
         end = timer()
         return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)
