@@ -122,8 +122,7 @@ class BatchedSimulation:
         for b, fl in enumerate(flows):
             n = q * int(np.prod(fl.resolution))
             o = int(dom[b]["offset"])
-            if fl._aa_pending:
-                fl._unpack_aa()
+            fl._settle()
             self._pools[0][o:o + n].copy_(fl.f_raw.reshape(-1))
         self._cur = 0
         self._domains_dev = torch.from_numpy(dom.view(np.uint8).copy()).to(dev)
@@ -236,6 +235,7 @@ class BatchedSimulation:
             o = int(self.domains[b]["offset"])
             fl._f = pool[o:o + n].view([q] + list(fl.resolution))
             fl._aa_pending = False
+            fl._stream_pending = None
 
     @property
     def status(self) -> int:

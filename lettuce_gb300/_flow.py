@@ -106,6 +106,10 @@ class Flow(ABC):
                               dtype=context.storage_dtype)
         self._f_next = None
         self._aa_pending = False
+        # a Simulation running POST_STREAMING as pull steps leaves the field
+        # post-collision with its stream still to apply: this is then the
+        # callable that applies it (see Simulation)
+        self._stream_pending = None
         self.initialize()
 
     # -- boundaries ------------------------------------------------------
@@ -144,8 +148,7 @@ class Flow(ABC):
         float64 storage this is the stored tensor itself; for the shifted
         16-bit formats it is a decoded float32 copy (assign ``flow.f = ...``
         to write)."""
-        if self._aa_pending:
-            self._unpack_aa()
+        self._settle()
         if self.context.shifted:
             return self._f.to(torch.float32) + _weights_view(self, torch.float32)
         return self._f
@@ -154,6 +157,7 @@ class Flow(ABC):
     def f(self, value: torch.Tensor):
         value = torch.as_tensor(value)
         self._aa_pending = False
+        self._stream_pending = None
         if self._upload_pinned(value):
             return
         if self.context.shifted:
@@ -201,8 +205,7 @@ class Flow(ABC):
         if self._host_transfer_ok(out):
             ptr = _device.host_device_pointer(out)
             if ptr is not None:
-                if self._aa_pending:
-                    self._unpack_aa()
+                self._settle()
                 _device.convert_ptr(self.stencil.lgb_id, self._f.data_ptr(), self.context.storage,
                                     ptr, _device.storage_of(out.dtype), out[0].numel(),
                                     torch.cuda.current_stream(self.context.device).cuda_stream)
@@ -238,8 +241,19 @@ class Flow(ABC):
         self._f = out
         self._aa_pending = False
 
+    def _settle(self):
+        """bring the stored field to lettuce's layout and time level: apply
+        a pending stream, or unpack an AA layout"""
+        if self._stream_pending is not None:
+            apply, self._stream_pending = self._stream_pending, None
+            apply()
+        if self._aa_pending:
+            self._unpack_aa()
+
     # -- moments (lettuce/_flow.py:157-204) ---------------------------------
     def _own_moments(self):
+        if self._stream_pending is not None:
+            self._settle()
         return _device.moments(self.stencil.lgb_id, self.context.storage, self.resolution,
                                self._f, self._aa_pending, self.context.dtype)
 

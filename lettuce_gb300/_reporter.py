@@ -31,6 +31,8 @@ def reduce_flow(flow, lo=None, hi=None, mask=None) -> torch.Tensor:
     m = None
     if mask is not None:
         m = torch.as_tensor(mask, device=flow.context.device).to(torch.uint8).contiguous()
+    if flow._stream_pending is not None:
+        flow._settle()
     return _device.reduce(flow.stencil.lgb_id, flow.context.storage, flow.resolution,
                           flow.f_raw, flow._aa_pending, lo, hi, m)
 

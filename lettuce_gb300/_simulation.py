@@ -160,10 +160,8 @@ def apply_local(flow, collision_native: NativeCollision,
         raise RuntimeError("lettuce_gb300 operators run on CUDA devices only; "
                            "there is no CPU path")
     natives = [collision_native] + ([boundary_native] if boundary_native else [])
-    src = flow.f_raw if not flow._aa_pending else None
-    if src is None:
-        flow._unpack_aa()
-        src = flow.f_raw
+    flow._settle()
+    src = flow.f_raw
     out = torch.empty_like(src)
     d, keep = _desc_for(flow, natives, flags, None, 0)
     d.pattern = _lib.LOCAL
@@ -185,11 +183,19 @@ class Simulation:
     launching every step from Python. ``None`` (default) enables it when the
     simulation has no reporters; with reporters and ``use_graph=True`` the
     reporters are called at the steps where one of them is due
-    (``flow.i % interval == 0``) instead of after every step."""
+    (``flow.i % interval == 0``) instead of after every step.
+    ``post_as_pull``: POST_STREAMING with two fields runs as one
+    collide-only launch followed by pull steps, the field left
+    post-collision with its stream pending until it is read (the
+    populations are the same as with the push kernels, bit for bit). None
+    (default) chooses it where the pull kernels measured faster: grids
+    without boundaries, and KBC. It applies while no reporter has an
+    interval below 8."""
 
     def __init__(self, flow, collision, reporter: List[Reporter],
                  streaming_strategy=StreamingStrategy.POST_STREAMING,
-                 memory_pattern: str = "ab", use_graph: Optional[bool] = None):
+                 memory_pattern: str = "ab", use_graph: Optional[bool] = None,
+                 post_as_pull: Optional[bool] = None):
         self.use_graph = use_graph
         self._graph = None
         self.flow = flow
@@ -260,6 +266,14 @@ class Simulation:
             if self._nsb is not None:
                 raise ValueError("the AA pattern does not support no-streaming masks "
                                  "(anti-bounce-back outlets); use memory_pattern='ab'")
+        self._pending_fn = self._apply_pending_stream
+        if post_as_pull is None:
+            # measured: the pull kernels are faster except for masked BGK/TRT
+            # runs, where the push kernel is 3 % ahead
+            post_as_pull = self._flags is None or self._desc.collision == _lib.KBC
+        self._post_pull_ok = (s == StreamingStrategy.POST_STREAMING and memory_pattern == "ab"
+                              and bool(post_as_pull))
+        self._pull_post = False
         if s == StreamingStrategy.PRE_STREAMING:
             self._patterns = [_lib.PULL]
         elif s == StreamingStrategy.POST_STREAMING:
@@ -268,6 +282,7 @@ class Simulation:
             self._patterns = [_lib.PULL, _lib.STREAM_ONLY]
         else:
             self._patterns = [_lib.LOCAL]
+        self._choose_pull_post()
 
     # ------------------------------------------------------------------
     @property
@@ -290,26 +305,61 @@ class Simulation:
         if stream is None:
             stream = self.context.stream_handle()
         if self.memory_pattern == "aa":
+            if flow._stream_pending is not None:
+                flow._settle()
             d.pattern = _lib.AA_ODD if flow._aa_pending else _lib.AA_EVEN
             d.f_in = d.f_out = flow._f.data_ptr()
             _device.step(d, stream)
             flow._aa_pending = not flow._aa_pending
             return
+        if self._pull_post:
+            # POST_STREAMING as pull steps: (S C)^n = S (C S)^(n-1) C. The
+            # field stays post-collision; its stream is applied when read.
+            if flow._stream_pending is not self._pending_fn:
+                flow._settle()
+                self._launch(_lib.LOCAL, stream)
+            else:
+                self._launch(_lib.PULL, stream)
+            flow._stream_pending = self._pending_fn
+            return
+        if flow._stream_pending is not None:
+            flow._settle()
         for pat in self._patterns:
-            src = flow._f
-            dst = flow.f_next
-            d.pattern = pat
-            d.f_in = src.data_ptr()
-            d.f_out = dst.data_ptr()
-            _device.step(d, stream)
-            flow._f, flow._f_next = dst, src
+            self._launch(pat, stream)
+
+    def _launch(self, pattern: int, stream: int):
+        """one launch of the step kernel, fields A -> B, then swapped"""
+        flow = self.flow
+        d = self._desc
+        src = flow._f
+        dst = flow.f_next
+        d.pattern = pattern
+        d.f_in = src.data_ptr()
+        d.f_out = dst.data_ptr()
+        _device.step(d, stream)
+        flow._f, flow._f_next = dst, src
+
+    def _apply_pending_stream(self):
+        """the stream a POST_STREAMING run left pending (one STREAM_ONLY
+        launch on the current stream)"""
+        self._launch(_lib.STREAM_ONLY, self.context.stream_handle())
+
+    def _choose_pull_post(self):
+        """POST_STREAMING runs as pull steps when reporters read the field
+        rarely enough (each read applies the pending stream and restarts
+        with a collide-only step): no reporters, or none with an interval
+        below 8"""
+        if not self._post_pull_ok:
+            self._pull_post = False
+            return
+        intervals = [int(getattr(r, "interval", 1) or 1) for r in self.reporter]
+        self._pull_post = all(iv >= 8 for iv in intervals)
 
     # -- the two halves of a step (lettuce/_simulation.py:245-305) ----------
     def _run_pattern(self, pattern: int) -> torch.Tensor:
         self._require_device()
         flow = self.flow
-        if flow._aa_pending:
-            flow._unpack_aa()
+        flow._settle()
         d = self._desc
         d.pattern = pattern
         src, dst = flow._f, flow.f_next
@@ -340,7 +390,7 @@ class Simulation:
         d = self._desc
         return (self.flow._f.data_ptr(),
                 self.flow._f_next.data_ptr() if self.flow._f_next is not None else 0,
-                self.flow._aa_pending,
+                self.flow._aa_pending, self.flow._stream_pending is not None,
                 ctypes.string_at(ctypes.addressof(d), ctypes.sizeof(d)))
 
     def _advance(self, n: int):
@@ -412,6 +462,7 @@ class Simulation:
 
     def __call__(self, num_steps: int) -> float:
         self._require_device()
+        self._choose_pull_post()
         beg = timer()
         if self.flow.i == 0:
             self._report()
@@ -431,6 +482,7 @@ class BreakableSimulation(Simulation):
 
     def __call__(self, num_steps: int) -> float:
         self._require_device()
+        self._choose_pull_post()
         beg = timer()
         if self.flow.i == 0:
             self._report()

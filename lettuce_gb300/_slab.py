@@ -178,6 +178,7 @@ class SlabSimulation:
         self.slabs = [Slab(flow.resolution[0], parts, i, e_x) for i in indices]
         if len(self.slabs) > 1 and len(self.slabs) != parts:
             raise ValueError("a process holds one part or all of them")
+        flow._settle()
         f = flow.f_raw
         self.f = [s.extend(f, 1).to(self.device) for s in self.slabs]
         self.f_next = [torch.empty_like(t) for t in self.f]

@@ -524,9 +524,13 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (p.abb_k >= 0 && d->f_in == d->f_out)
         return fail("lgb_step: the anti-bounce-back outlet reads its neighbour plane and "
                     "needs distinct input and output fields");
-    // the kernel variant: BGK with a force is its own collision kind
-    const int coll = d->collision == LGB_BGK && d->force != LGB_FORCE_NONE ? lgb::LGB_BGK_FORCED
-                                                                            : d->collision;
+    // the kernel variant: BGK with a force is its own collision kind; the
+    // patterns without a collision (stream only, AA unpack) run as such
+    // whatever the descriptor's collision
+    const bool no_coll = d->pattern == LGB_STREAM_ONLY || d->pattern == LGB_AA_UNPACK;
+    const int coll = no_coll ? LGB_NO_COLLISION
+                     : (d->collision == LGB_BGK && d->force != LGB_FORCE_NONE ? lgb::LGB_BGK_FORCED
+                                                                              : d->collision);
     const bool vec2 = !(d->options & LGB_OPT_ONE_CELL) &&
                       use_vec2(d->storage, coll, d->pattern, masked, g.Z);
     cudaError_t e = vec2

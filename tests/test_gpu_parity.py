@@ -290,7 +290,7 @@ def test_two_cell_kernel_bit_identical(lgb, storage, S, res, coll, pattern):
         c = lt.BGKCollision(tau) if coll == "bgk" else lt.TRTCollision(tau, 0.8)
         kw = {"memory_pattern": "aa"} if pattern == "aa" else {
             "streaming_strategy": lt.StreamingStrategy.PRE_STREAMING if pattern == "pull"
-            else lt.StreamingStrategy.POST_STREAMING}
+            else lt.StreamingStrategy.POST_STREAMING, "post_as_pull": False}
         sim = lt.Simulation(flow, c, [], **kw)
         sim._desc.options = options
         sim(7)
@@ -311,7 +311,7 @@ def test_two_cell_kernel_tiny_rows(lgb, res, pattern):
         flow = GivenFlow(c, lt.D3Q19(), f0)
         kw = ({"memory_pattern": "aa"} if pattern == "aa" else
               {"streaming_strategy": STRATS["PRE_STREAMING" if pattern == "pull"
-                                            else "POST_STREAMING"]})
+                                            else "POST_STREAMING"], "post_as_pull": False})
         sim = lt.Simulation(flow, lt.BGKCollision(0.6), [], use_graph=False, **kw)
         if one_cell:
             sim._desc.options |= _lib.OPT_ONE_CELL
@@ -400,7 +400,8 @@ def test_push_guard_bit_identical(lgb, name):
             flow = obstacle_flow(ctx(F64), z, m)
         coll = lt.KBCCollision() if m["collision"] == "kbc" else \
             lt.BGKCollision(flow.units.relaxation_parameter_lu)
-        sim = lt.Simulation(flow, coll, [], streaming_strategy=lt.StreamingStrategy.POST_STREAMING)
+        sim = lt.Simulation(flow, coll, [], streaming_strategy=lt.StreamingStrategy.POST_STREAMING,
+                            post_as_pull=False)
         from lettuce_gb300 import _lib
         assert sim._desc.options & _lib.OPT_PUSH_GUARD
         if not guard:
@@ -571,3 +572,81 @@ def test_collide_and_stream_halves(lgb, name):
             for h in halves:
                 getattr(sb, h)()
         assert torch.equal(a.f, b.f), strategy
+
+
+@pytest.mark.parametrize("name", golden_names("obstacle") + golden_names("outletp"))
+def test_post_as_pull_bit_identical(lgb, name):
+    """POST_STREAMING run as a collide-only launch plus pull steps (the
+    stream applied when the field is read) equals the push kernels bit for
+    bit, with every boundary of the flow; reporters with short intervals
+    switch it off, long ones keep it"""
+    z = golden(name)
+    m = meta(z)
+
+    def make():
+        if name.startswith("outletp"):
+            _ObstacleP.rho_outlet = m["rho_outlet"]
+            flow = _ObstacleP(ctx(F32), m["res"], m["re"], m["ma"], m["domain_length_x"],
+                              stencil=getattr(lt, m["stencil"]))
+            flow.mask = z["mask"]
+            flow.initialize()
+            return flow
+        return obstacle_flow(ctx(F32), z, m)
+
+    def coll(fl):
+        return lt.KBCCollision() if m.get("collision") == "kbc" else \
+            lt.BGKCollision(fl.units.relaxation_parameter_lu)
+
+    post = lt.StreamingStrategy.POST_STREAMING
+    a, b = make(), make()
+    sa = lt.Simulation(a, coll(a), [], streaming_strategy=post, post_as_pull=False)
+    sb = lt.Simulation(b, coll(b), [], streaming_strategy=post, post_as_pull=True)
+    assert sb._pull_post and not sa._pull_post
+    # the automatic choice: pull for KBC, push for masked BGK
+    auto = lt.Simulation(make(), coll(b), [], streaming_strategy=post)
+    assert auto._pull_post == (m.get("collision") == "kbc")
+    sa(9)
+    sb(9)
+    assert b._stream_pending is not None
+    assert torch.equal(a.f, b.f) and b._stream_pending is None
+    # observables read through the pending stream
+    sa(5)
+    sb(5)
+    assert torch.equal(lt.IncompressibleKineticEnergy(b)(), lt.IncompressibleKineticEnergy(a)())
+    # a reporter every step switches the mode off; every 10 steps keeps it
+    for iv, expect in ((1, False), (10, True)):
+        c = make()
+        rep = lt.ObservableReporter(lt.MaximumVelocity(c), interval=iv, out=None)
+        sc = lt.Simulation(c, coll(c), [rep], streaming_strategy=post, post_as_pull=True)
+        assert sc._pull_post == expect
+        sc(20)
+        d = make()
+        lt.Simulation(d, coll(d), [], streaming_strategy=post, post_as_pull=False)(20)
+        assert torch.equal(c.f, d.f)
+
+
+@pytest.mark.parametrize("storage", [None, "fp16_shifted"])
+def test_post_as_pull_periodic(lgb, storage):
+    """the same on a periodic Taylor-Green vortex (two-cell kernel for fp16)"""
+    outs = []
+    for pap in (False, True):
+        flow = lt.TaylorGreenVortex(ctx(F32, storage), [24, 20, 16], 400, 0.05, lt.D3Q19)
+        lt.Simulation(flow, lt.BGKCollision(flow.units.relaxation_parameter_lu), [],
+                      streaming_strategy=lt.StreamingStrategy.POST_STREAMING,
+                      post_as_pull=pap)(11)
+        outs.append(flow.f.clone())
+    assert torch.equal(outs[0], outs[1])
+
+
+def test_double_streaming_with_force(lgb, oracle):
+    """DOUBLE_STREAMING (pull, then a collision-free stream) with a forced
+    collision: the stream launch runs as a plain stream"""
+    z = golden("ext_d2q9_bgk_guo")
+    m = meta(z)
+    flow = GivenFlow(ctx(F64), lt.D2Q9(), z["f0"])
+    coll = _ext_collision("bgk_guo", flow, z, m)
+    lt.Simulation(flow, coll, [], streaming_strategy=lt.StreamingStrategy.DOUBLE_STREAMING)(3)
+    ref = oracle.run("D2Q9", z["f0"], 3, collision="bgk", tau=float(z["tau"]),
+                     strategy="DOUBLE_STREAMING", force="guo", force_tau=float(z["force_tau"]),
+                     accel=z["accel"])
+    assert rel_max(to_np(flow.f), ref) < 1e-12

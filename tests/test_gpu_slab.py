@@ -32,6 +32,7 @@ def compare(make_flow, make_collision, parts, strategy, steps=7, boundaries=None
     sim(steps)
     slabs(steps)
     torch.cuda.synchronize()
+    flow_a._settle()
     whole = flow_a.f_raw
     split = slabs.gather()
     assert split.shape == whole.shape
