@@ -409,11 +409,15 @@ class Simulation:
         if g is None:
             # two eager steps (they count), then capture a pair of steps that
             # returns the fields to the same assignment; graphs are kept per
-            # field assignment (both parities of A/B, both AA phases)
+            # field assignment (both parities of A/B, both AA phases). The
+            # eager steps may reach a state captured before (a stream that was
+            # applied for a reporter is pending again after them).
             for _ in range(2):
                 self._collide_and_stream(self)
                 flow.i += 1
             n -= 2
+            g = self._graph.get(self._state_key())
+        if g is None:
             def pair(stream):
                 self._collide_and_stream(self, stream=stream)
                 self._collide_and_stream(self, stream=stream)

@@ -84,3 +84,22 @@ def test_graph_default_off_with_reporters(lgb):
     assert [r[0] for r in rep.out] == [0, 1, 2, 3]
     sim2 = lt.Simulation(tgv(), lt.BGKCollision(0.6), [])
     assert sim2._graphs_enabled()
+
+
+def test_graph_with_post_as_pull_and_reporters(lgb):
+    """POST_STREAMING as pull steps, replayed from graphs, with a reporter
+    every 10 steps (each report applies the pending stream): the same
+    populations and reports as the push kernels launched step by step"""
+    outs, reps = [], []
+    for use_graph, pap in ((False, False), (True, True)):
+        flow = tgv()
+        rep = lt.ObservableReporter(lt.IncompressibleKineticEnergy(flow), interval=10, out=None)
+        sim = lt.Simulation(flow, lt.BGKCollision(flow.units.relaxation_parameter_lu), [rep],
+                            streaming_strategy=S.POST_STREAMING, use_graph=use_graph,
+                            post_as_pull=pap)
+        assert sim._pull_post == pap
+        sim(47)
+        outs.append(flow.f.clone())
+        reps.append(np.array(rep.out))
+    assert torch.equal(outs[0], outs[1])
+    assert np.array_equal(reps[0], reps[1]) and len(reps[0]) == 5
