@@ -78,6 +78,67 @@ int make_grid(int stencil, const int32_t *res, Grid *g) {
 
 bool valid_storage(int s) { return s >= LGB_F64 && s <= LGB_BF16_SHIFTED; }
 
+// per host thread and device: a second stream and the two events of a
+// fork/join (per thread, so that concurrent callers do not reorder each
+// other's events). Created on first use outside a stream capture.
+struct AuxStream {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+thread_local AuxStream g_aux[64];
+
+}  // namespace
+
+namespace lgb {
+cudaStream_t fork_aux(cudaStream_t s) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    AuxStream &a = g_aux[dev];
+    if (!a.stream) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        cudaStream_t st = nullptr;
+        cudaEvent_t ef = nullptr, ej = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ef, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ej, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            if (ef) cudaEventDestroy(ef);
+            if (st) cudaStreamDestroy(st);
+            return nullptr;
+        }
+        a.stream = st;
+        a.fork = ef;
+        a.join = ej;
+    }
+    if (cudaEventRecord(a.fork, s) != cudaSuccess ||
+        cudaStreamWaitEvent(a.stream, a.fork, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.stream;
+}
+
+cudaError_t join_aux(cudaStream_t s, cudaStream_t aux) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    AuxStream &a = g_aux[dev];
+    if (aux != a.stream) return cudaErrorInvalidValue;
+    e = cudaEventRecord(a.join, aux);
+    if (e != cudaSuccess) return e;
+    return cudaStreamWaitEvent(s, a.join, 0);
+}
+}  // namespace lgb
+
+namespace {
+
 cudaError_t dispatch_step(int stencil, int storage, int coll, int pat, bool masked,
                           const lgb::StepParams &p, cudaStream_t s) {
 #define LGB_STORAGE_SWITCH(name)                                            \

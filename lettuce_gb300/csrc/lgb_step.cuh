@@ -458,19 +458,37 @@ template <int SID> constexpr bool has_kbc() { return SID == LGB_D2Q9 || SID == L
 
 // with boundaries: the bulk launch (MASK 1) and, if there is an outlet and
 // the pattern has substeps, the outlet-plane launch (MASK 2)
+// A second stream of the current device ordered after `s` (fork), and the
+// join of its work back into `s` (lgb_abi.cu). fork_aux returns nullptr
+// where no second stream is available; the caller then stays on `s`.
+cudaStream_t fork_aux(cudaStream_t s);
+cudaError_t join_aux(cudaStream_t s, cudaStream_t aux);
+
 template <int SID, int ST, int COLL, int PAT, bool MASKED>
 cudaError_t launch_step_set(const StepParams &p, cudaStream_t s) {
     if constexpr (!MASKED) {
         return launch_step<SID, ST, COLL, PAT, 0>(p, s);
     } else {
-        cudaError_t e = launch_step<SID, ST, COLL, PAT, 1>(p, s);
-        if (e != cudaSuccess) return e;
         constexpr bool SUBSTEPS = PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK;
         constexpr bool OUTLET = SUBSTEPS && PAT != LGB_AA_EVEN && PAT != LGB_AA_ODD;
         if constexpr (OUTLET) {
-            if (p.abb_k >= 0) return launch_step<SID, ST, COLL, PAT, 2>(p, s);
+            if (p.abb_k >= 0) {
+                // the outlet plane and the bulk write disjoint populations
+                // (every destination slot has one writer) and only read the
+                // input field: the short plane launch runs beside the bulk
+                cudaStream_t aux = fork_aux(s);
+                if (aux) {
+                    const cudaError_t e2 = launch_step<SID, ST, COLL, PAT, 2>(p, aux);
+                    const cudaError_t e1 = launch_step<SID, ST, COLL, PAT, 1>(p, s);
+                    const cudaError_t e3 = join_aux(s, aux);
+                    return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+                }
+                const cudaError_t e = launch_step<SID, ST, COLL, PAT, 1>(p, s);
+                if (e != cudaSuccess) return e;
+                return launch_step<SID, ST, COLL, PAT, 2>(p, s);
+            }
         }
-        return cudaSuccess;
+        return launch_step<SID, ST, COLL, PAT, 1>(p, s);
     }
 }
 
