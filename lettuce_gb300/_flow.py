@@ -184,8 +184,17 @@ class Flow(ABC):
         ptr = _device.host_device_pointer(value)
         if ptr is None:
             return False
-        out = torch.empty([self.stencil.q] + list(self.resolution),
-                          dtype=self.context.storage_dtype, device=self.context.device)
+        shape = [self.stencil.q] + list(self.resolution)
+        spare = self._f_next
+        if (spare is not None and list(spare.shape) == shape
+                and spare.dtype == self.context.storage_dtype
+                and spare.data_ptr() != self._f.data_ptr()):
+            # the second field is scratch between steps: upload into it and
+            # keep the pair of buffers (captured step graphs stay valid)
+            out, self._f_next = spare, self._f
+        else:
+            out = torch.empty(shape, dtype=self.context.storage_dtype,
+                              device=self.context.device)
         _device.convert_ptr(self.stencil.lgb_id, ptr, _device.storage_of(value.dtype),
                             out.data_ptr(), self.context.storage, out[0].numel(),
                             torch.cuda.current_stream(self.context.device).cuda_stream)

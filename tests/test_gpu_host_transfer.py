@@ -70,3 +70,22 @@ def test_host_pointer_on_pageable_memory(lgb):
     flow = tgv(torch.float32)
     lt.Simulation(flow, lt.BGKCollision(0.6), [])(2)
     torch.cuda.synchronize()
+
+
+def test_pinned_upload_reuses_the_second_field(lgb):
+    """after steps, an upload goes into the scratch field: the simulation
+    keeps its two buffers (and its captured graphs) and continues exactly
+    as after a torch upload"""
+    a, b = tgv(torch.float32), tgv(torch.float32)
+    sa = lt.Simulation(a, lt.BGKCollision(0.6), [])
+    sb = lt.Simulation(b, lt.BGKCollision(0.6), [])
+    sa(6)
+    sb(6)
+    bufs = {a._f.data_ptr(), a._f_next.data_ptr()}
+    host = (a.f.cpu() * 1.001).pin_memory()
+    a.f = host
+    b.f = host.to("cuda:0")
+    assert {a._f.data_ptr(), a._f_next.data_ptr()} == bufs
+    sa(6)
+    sb(6)
+    assert torch.equal(a.f, b.f)
