@@ -4,7 +4,10 @@
  * Plain C: device pointers, sizes and scalars only. Every call is
  * asynchronous on the CUDA stream it is given (a cudaStream_t passed as
  * void*, NULL = legacy default stream); nothing here allocates device memory
- * or synchronises. Errors: a non-zero return code and a message from
+ * or synchronises. (lgb_step creates, once per host thread and device and
+ * outside stream captures, a second stream and two events: a step with an
+ * outlet plane runs the plane's launch on it, forked from and joined back
+ * into the given stream.) Errors: a non-zero return code and a message from
  * lgb_last_error(); no call traps or aborts on the device.
  *
  * Layout of a population field: lettuce's [Q, *resolution], C-contiguous,

@@ -153,9 +153,9 @@ __device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
 #define LGB_VEC2_MIN_BLOCKS 4
 #endif
 // D2Q9 and D1Q3 (9 and 3 populations) need fewer registers: more blocks
-// (measured on D2Q9 4096^2 fp16: 5 blocks 154.5k MLUPS against 141.1k at 4)
+// (measured on D2Q9 4096^2 fp16: 6 blocks 160.7k MLUPS, 5 blocks 154.1k, 4 blocks 141.1k)
 #ifndef LGB_VEC2_2D_MIN_BLOCKS
-#define LGB_VEC2_2D_MIN_BLOCKS 5
+#define LGB_VEC2_2D_MIN_BLOCKS 6
 #endif
 template <int SID>
 constexpr int vec2_min_blocks() {
