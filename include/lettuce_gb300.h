@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LGB_ABI_VERSION 2
+#define LGB_ABI_VERSION 3
 #define LGB_MAX_SUBSTEPS 8
 
 /* stencils (lettuce/ext/_stencil/d1q3.py, d2q9.py, d3q15.py, d3q19.py, d3q27.py) */
@@ -83,8 +83,10 @@ enum {
 /* per-cell flag byte: low 5 bits = substep index (lettuce's
  * no_collision_mask value); bit 7 = the cell has no-streaming bits; bit 6 =
  * some neighbour x + e_q does not stream population q (read only under
- * LGB_OPT_PUSH_GUARD) */
+ * LGB_OPT_PUSH_GUARD); bit 5 = the cell has halfway bounce-back links
+ * (read only when the descriptor's link_bits is set) */
 #define LGB_FLAG_INDEX_MASK 0x1f
+#define LGB_FLAG_LINKS 0x20
 #define LGB_FLAG_PUSH_GUARD 0x40
 #define LGB_FLAG_NO_STREAM 0x80
 
@@ -135,6 +137,26 @@ typedef struct {
                                  moment matrix M [Q][Q] (row-major), its inverse
                                  [Q][Q] and the Q relaxation times s_i
                                  (m_i <- m_i - (m_i - meq_i) / s_i) */
+    /* Halfway bounce-back of the post-streaming boundaries of lettuce's
+     * example project (examples/advanced_projects/efficient_bounce_back_obstacle/
+     * boundary/halfway_bounce_back_boundary.py:170-242, applied after the
+     * stream by simulation/ebb_simulation.py:72-101). Patterns that stream
+     * by pulling (LGB_PULL, LGB_STREAM_ONLY) read link_bits[n] at the cells
+     * whose flags carry LGB_FLAG_LINKS: bit q set = population q is not
+     * pulled from x - e_q (a solid cell) but takes the cell's own
+     * post-collision population opp(q). NULL = no links. */
+    const uint32_t *link_bits;   /* [N] */
+    /* Momentum exchange on the links of one boundary
+     * (halfway_bounce_back_boundary.py:211-218): force_links holds
+     * n_force_links pairs (q, n), q pointing from fluid cell n into the
+     * solid. LGB_PULL and LGB_STREAM_ONLY launches, whose stream crosses the
+     * links, write 2 sum f*_q(n) e_q (f* = the post-collision field f_in)
+     * to force_out (float64 [3], lattice units, lettuce dimension order;
+     * unused trailing entries 0); LGB_LOCAL leaves it. Device memory;
+     * NULL / 0 = not computed. */
+    const uint32_t *force_links; /* [n_force_links][2] */
+    int64_t n_force_links;
+    double *force_out;
 } lgb_step_desc;
 
 /* options: run the one-cell-per-thread kernel even where the two-cell

@@ -18,8 +18,10 @@ from ._collision import (BGKCollision, Collision, KBCCollision, MRTCollision, No
 from ._moments import D1Q3Transform, D2Q9Dellar, D2Q9Lallemand, D3Q27Hermite, Transform
 from ._force import Force, Guo, ShanChen
 from ._boundary import (AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU,
-                        EquilibriumOutletP, PartiallySaturatedBC)
-from ._simulation import BreakableSimulation, Reporter, Simulation, StreamingStrategy
+                        EquilibriumOutletP, HalfwayBounceBackBoundary, PartiallySaturatedBC,
+                        SolidBoundaryData, hwbb_links)
+from ._simulation import (BreakableSimulation, EbbSimulation, Reporter, Simulation,
+                          StreamingStrategy)
 from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporterBase,
                         HighMaReporter, IncompressibleKineticEnergy, Mass,
                         MaximumVelocity, NaNReporter, Observable, ObservableReporter)
@@ -37,7 +39,8 @@ __all__ = [
     "initialize_f_neq", "torch_gradient", "Collision", "BGKCollision",
     "TRTCollision", "KBCCollision", "NoCollision", "BounceBackBoundary",
     "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "EquilibriumOutletP",
-    "PartiallySaturatedBC", "Simulation",
+    "PartiallySaturatedBC", "HalfwayBounceBackBoundary", "SolidBoundaryData", "hwbb_links",
+    "Simulation", "EbbSimulation",
     "BreakableSimulation", "StreamingStrategy", "Reporter", "Observable",
     "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",
     "Enstrophy", "EnergySpectrum", "Mass", "ErrorReporter", "FailureReporterBase",

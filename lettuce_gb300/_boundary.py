@@ -5,6 +5,10 @@
 * AntiBounceBackOutlet -- lettuce/ext/_boundary/anti_bounce_back_outlet.py:13-109
 * EquilibriumOutletP -- lettuce/ext/_boundary/equilibrium_outlet_p.py:12-91
 * PartiallySaturatedBC -- lettuce/ext/_boundary/partially_saturated_boundary.py:6-51
+* HalfwayBounceBackBoundary, SolidBoundaryData -- lettuce's example project
+  examples/advanced_projects/efficient_bounce_back_obstacle/boundary/
+  halfway_bounce_back_boundary.py:10-254 and solid_boundary_data.py:7-14; a
+  post-streaming boundary, run by ``EbbSimulation``
 
 The masks are built exactly as lettuce builds them (they are combined by
 ``Simulation`` into the per-cell flag byte); the operators themselves run
@@ -24,7 +28,8 @@ from ._flow import Boundary
 from ._native import NativeBoundary, NativeCollision
 
 __all__ = ["BounceBackBoundary", "EquilibriumBoundaryPU", "AntiBounceBackOutlet",
-           "EquilibriumOutletP", "PartiallySaturatedBC"]
+           "EquilibriumOutletP", "PartiallySaturatedBC", "SolidBoundaryData",
+           "HalfwayBounceBackBoundary", "hwbb_links"]
 
 
 def _apply_alone(flow, native: NativeBoundary, flags_value):
@@ -217,3 +222,140 @@ class PartiallySaturatedBC(Boundary):
     def native_generator(self, index: int) -> NativeBoundary:
         return NativeBoundary(_lib.SUB_PARTIALLY_SATURATED, index,
                               params=(float(self.tau), float(self.B)))
+
+
+class SolidBoundaryData(dict):
+    """The solid description of the example project's bounce-back boundaries
+    (solid_boundary_data.py:7-14): ``solid_mask`` and, optionally, the link
+    lists ``f_index_lt`` / ``f_index_gt`` (rows q, x, y[, z]; q points from
+    the fluid cell into the solid) with their wall distances ``d_lt`` /
+    ``d_gt``. Attributes are set by the caller."""
+
+
+def _to_numpy_bool(m) -> np.ndarray:
+    if isinstance(m, torch.Tensor):
+        return m.detach().cpu().numpy().astype(bool)
+    return np.asarray(m, dtype=bool)
+
+
+def hwbb_links(e, opposite, mask, global_solid_mask=None, periodicity=None) -> np.ndarray:
+    """The link list of the halfway bounce-back's neighbour search
+    (halfway_bounce_back_boundary.py:70-161), rows (q, x, y[, z]) in its
+    order: for every solid cell p of ``mask`` (``np.where`` order) and every
+    velocity i, the neighbour c = p + e_i. Along an axis marked periodic c
+    wraps around; along the others a c past the upper end drops the link,
+    and c = -1 is kept as written (Python indexing reads the last cell
+    there, so the link acts on that cell). A neighbour that is solid neither
+    in ``mask`` nor in ``global_solid_mask`` (default: ``mask``) gives the
+    link (opposite[i], c)."""
+    mask = _to_numpy_bool(mask)
+    gmask = mask if global_solid_mask is None else _to_numpy_bool(global_solid_mask)
+    e = np.asarray(e, dtype=np.int64)
+    opp = np.asarray(opposite, dtype=np.int64)
+    dims = mask.ndim
+    if periodicity is None:
+        periodicity = (False,) * dims
+    shape = np.array(mask.shape, dtype=np.int64)
+    p = np.stack(np.nonzero(mask), axis=1).astype(np.int64)          # [P, D]
+    c = p[:, None, :] + e[None, :, :dims]                            # [P, Q, D]
+    ok = np.ones(c.shape[:2], dtype=bool)
+    for k in range(dims):
+        if periodicity[k]:
+            # the search's border shift: only -1 and n occur (|e| <= 1)
+            c[..., k] = np.where(c[..., k] < 0, c[..., k] + shape[k],
+                                 np.where(c[..., k] >= shape[k], c[..., k] - shape[k], c[..., k]))
+        else:
+            ok &= c[..., k] < shape[k]
+    wrapped = np.where(c < 0, c + shape, c)
+    wrapped = np.where(ok[..., None], wrapped, 0)
+    idx = tuple(wrapped[..., k] for k in range(dims))
+    ok &= ~mask[idx] & ~gmask[idx]
+    q = np.broadcast_to(opp[None, :], ok.shape)
+    rows = np.concatenate([q[..., None], c], axis=-1)[ok]
+    return rows.reshape(-1, dims + 1).astype(np.int64)
+
+
+class HalfwayBounceBackBoundary(Boundary):
+    """Halfway bounce-back with momentum exchange (the example project's
+    HWBB, halfway_bounce_back_boundary.py:10-254). The solid cells neither
+    collide nor stream; after each step's stream, every fluid cell x next to
+    the solid takes for population opp(q) its own post-collision value of
+    population q, for each link q pointing into the solid. With
+    ``calc_force`` the momentum exchange 2 sum f*_q(x) e_q of the step's
+    links (lattice units) is kept as ``force_sum``.
+
+    The bounce runs inside the step kernel's pull (``EbbSimulation``); the
+    links are those of ``solid_boundary_data.f_index_lt`` /
+    ``f_index_gt`` when given, else of the neighbour search of
+    ``hwbb_links``."""
+
+    def __init__(self, context, flow, solid_boundary_data, global_solid_mask=None,
+                 periodicity=None, calc_force: bool = False):
+        self.context = context
+        self.flow = flow
+        self.mask = _to_numpy_bool(solid_boundary_data.solid_mask)
+        st = flow.stencil
+        if periodicity is None:
+            periodicity = (False, False, False if st.d == 3 else None)
+        lists = [np.asarray(getattr(solid_boundary_data, a)) for a in ("f_index_lt", "f_index_gt")
+                 if hasattr(solid_boundary_data, a)]
+        lists = [a.reshape(-1, st.d + 1) for a in lists if a.size]
+        if lists:
+            links = np.concatenate(lists, axis=0).astype(np.int64)
+        else:
+            links = hwbb_links(st.e, st.opposite, self.mask, global_solid_mask,
+                               tuple(periodicity)[:st.d])
+        self.f_index = torch.as_tensor(links, dtype=torch.int64, device=context.device)
+        self.calc_force = bool(calc_force)
+        self._force = None
+        if self.calc_force:
+            self._force = torch.zeros(3, dtype=torch.float64, device=context.device)
+
+    @property
+    def force_sum(self) -> torch.Tensor:
+        """momentum-exchange force of the last step's links, [D], context
+        dtype (lattice units); reading it applies a pending stream"""
+        if self._force is None:
+            raise AttributeError("force_sum needs calc_force=True")
+        self.flow._settle()
+        return self._force[:self.flow.stencil.d].to(self.context.dtype)
+
+    def link_bits(self) -> torch.Tensor:
+        """int32 [*res]: bit opp(q) set at fluid cell x for every link
+        (q, x); the pull at x then takes its own population q for opp(q)"""
+        st = self.flow.stencil
+        res = list(self.flow.resolution)
+        fi = self.f_index.detach().cpu().numpy()
+        bits = np.zeros(res, dtype=np.int64)
+        if len(fi):
+            opp = np.asarray(st.opposite, dtype=np.int64)
+            cells = np.where(fi[:, 1:] < 0, fi[:, 1:] + np.array(res), fi[:, 1:])
+            np.bitwise_or.at(bits, tuple(cells.T), np.left_shift(1, opp[fi[:, 0]]))
+        return torch.as_tensor(bits.astype(np.uint32).view(np.int32),
+                               device=self.context.device).contiguous()
+
+    def force_links(self) -> torch.Tensor:
+        """uint32 pairs [n, 2] (q, flat cell index) of the links, as int32
+        (the device list the momentum-exchange kernel reads)"""
+        res = list(self.flow.resolution)
+        fi = self.f_index.detach().cpu().numpy()
+        cells = np.where(fi[:, 1:] < 0, fi[:, 1:] + np.array(res), fi[:, 1:])
+        flat = np.ravel_multi_index(tuple(cells.T), tuple(res)) if len(fi) else np.zeros(0, int)
+        pairs = np.stack([fi[:, 0], flat], axis=1).astype(np.uint32).view(np.int32)
+        return torch.as_tensor(np.ascontiguousarray(pairs), device=self.context.device)
+
+    def __call__(self, flow):
+        raise RuntimeError("the halfway bounce-back runs inside the step of an EbbSimulation")
+
+    def make_no_collision_mask(self, shape: List[int], context) -> torch.Tensor:
+        return torch.as_tensor(self.mask, device=context.device)
+
+    def make_no_streaming_mask(self, shape: List[int], context) -> torch.Tensor:
+        return torch.as_tensor(self.mask, device=context.device)
+
+    def native_available(self) -> bool:
+        return True
+
+    def native_generator(self, index: int) -> NativeBoundary:
+        # the solid cells run no substep; the links travel as bits
+        return NativeBoundary(_lib.SUB_NONE, index)

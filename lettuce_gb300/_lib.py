@@ -12,7 +12,7 @@ import threading
 
 from . import build as _build
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_SUBSTEPS = 8
 REDUCE_FIELDS = 5
 
@@ -25,7 +25,7 @@ FORCE_NONE, FORCE_GUO, FORCE_SHAN_CHEN = 0, 1, 2
 SUB_COLLISION, SUB_BOUNCE_BACK, SUB_EQUILIBRIUM_PU, SUB_ANTI_BOUNCE_BACK, SUB_NONE = 0, 1, 2, 3, 4
 SUB_EQUILIBRIUM_OUTLET_P, SUB_PARTIALLY_SATURATED = 5, 6
 PULL, PUSH, LOCAL, AA_EVEN, AA_ODD, STREAM_ONLY, AA_UNPACK = 0, 1, 2, 3, 4, 5, 6
-FLAG_INDEX_MASK, FLAG_PUSH_GUARD, FLAG_NO_STREAM = 0x1F, 0x40, 0x80
+FLAG_INDEX_MASK, FLAG_LINKS, FLAG_PUSH_GUARD, FLAG_NO_STREAM = 0x1F, 0x20, 0x40, 0x80
 OPT_ONE_CELL, OPT_PUSH_GUARD = 1, 2
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
@@ -70,7 +70,11 @@ class StepDesc(ctypes.Structure):
                 ("smagorinsky_constant", ctypes.c_double),
                 ("mrt_equilibrium", ctypes.c_int32),
                 ("reserved2", ctypes.c_int32),
-                ("mrt_tables", ctypes.c_void_p)]
+                ("mrt_tables", ctypes.c_void_p),
+                ("link_bits", ctypes.c_void_p),
+                ("force_links", ctypes.c_void_p),
+                ("n_force_links", ctypes.c_int64),
+                ("force_out", ctypes.c_void_p)]
 
 
 class LibraryError(RuntimeError):

@@ -232,6 +232,7 @@ class Simulation:
                 if nsm is not None:
                     self.no_streaming_mask |= torch.as_tensor(
                         nsm, device=self.context.device).to(torch.uint8)
+        self._extend_masks(shape_f)
 
         # native descriptors (no fallback: every component must have one)
         missing = [c.__class__.__name__ for c in self.transformer if not c.native_available()]
@@ -254,6 +255,7 @@ class Simulation:
                                            self.collision_index)
         if self._nsb is not None:
             self._desc.options |= _lib.OPT_PUSH_GUARD
+        self._extend_desc()
         self._status = None
         if self.context.device.type == "cuda":
             self._status = torch.zeros(1, dtype=torch.int32, device=self.context.device)
@@ -283,6 +285,12 @@ class Simulation:
         else:
             self._patterns = [_lib.LOCAL]
         self._choose_pull_post()
+
+    def _extend_masks(self, shape_f):
+        """hook: masks of boundaries outside lettuce's pre/post lists"""
+
+    def _extend_desc(self):
+        """hook: descriptor fields of boundaries outside the substep list"""
 
     # ------------------------------------------------------------------
     @property
@@ -494,3 +502,86 @@ class BreakableSimulation(Simulation):
         self.context.synchronize()
         end = timer()
         return num_steps * self.flow._f[0].numel() / 1e6 / (end - beg)
+
+
+class EbbSimulation(Simulation):
+    """The simulation of lettuce's example project for efficient bounce-back
+    (examples/advanced_projects/efficient_bounce_back_obstacle/simulation/
+    ebb_simulation.py:11-105): every step collides, streams and then applies
+    the flow's post-streaming boundaries (``flow.post_streaming_boundaries``
+    when the flow's class defines it), whatever streaming strategy would
+    otherwise apply.
+
+    Masks follow ebb_simulation.py:28-57: the post-streaming boundaries'
+    cells take the substep indices after the post-collision boundaries (so
+    they neither collide nor run a boundary) and do not stream. The bounce
+    of ``HalfwayBounceBackBoundary`` runs inside the pull of the step kernel
+    (per-cell link bits), so the steps run as one collide-only launch
+    followed by pull launches, the last stream and bounce pending until the
+    field is read; ``_stream()`` called directly bounces as well. One
+    post-streaming boundary may compute its force."""
+
+    def __init__(self, flow, collision, reporter: List[Reporter],
+                 use_graph: Optional[bool] = None):
+        from ._boundary import HalfwayBounceBackBoundary
+        psb = []
+        if hasattr(flow.__class__, "post_streaming_boundaries"):
+            psb = list(flow.post_streaming_boundaries or [])
+        other = [b.__class__.__name__ for b in psb
+                 if not isinstance(b, HalfwayBounceBackBoundary)]
+        if other:
+            raise NotImplementedError(
+                f"no GB300 kernel for the post-streaming boundary {', '.join(other)}")
+        if sum(1 for b in psb if b.calc_force) > 1:
+            raise NotImplementedError("one post-streaming boundary per simulation may "
+                                      "compute its force")
+        self.post_streaming_boundaries = psb
+        self._link_bits = self._force_links = None
+        super().__init__(flow, collision, reporter,
+                         streaming_strategy=StreamingStrategy.POST_STREAMING,
+                         memory_pattern="ab", use_graph=use_graph, post_as_pull=True)
+
+    def _extend_masks(self, shape_f):
+        psb = self.post_streaming_boundaries
+        if not psb:
+            return
+        flow = self.flow
+        if self.no_collision_mask is None:
+            self.no_collision_mask = self.context.full_tensor(
+                flow.resolution, self.collision_index, dtype=torch.uint8)
+        if self.no_streaming_mask is None:
+            self.no_streaming_mask = self.context.full_tensor(
+                shape_f, self.collision_index, dtype=torch.uint8)
+        start = self.collision_index + 1 + len(self.post_boundaries)
+        for i, b in enumerate(psb, start=start):
+            ncm = b.make_no_collision_mask(list(flow.resolution), context=self.context)
+            if ncm is not None:
+                self.no_collision_mask[torch.as_tensor(ncm, device=self.context.device).bool()] = i
+            nsm = b.make_no_streaming_mask(shape_f, context=self.context)
+            if nsm is not None:
+                self.no_streaming_mask |= torch.as_tensor(
+                    nsm, device=self.context.device).to(torch.uint8)
+
+    def _extend_desc(self):
+        psb = self.post_streaming_boundaries
+        if not psb:
+            return
+        d = self._desc
+        bits = psb[0].link_bits()
+        for b in psb[1:]:
+            bits = bits | b.link_bits()
+        self._link_bits = bits.contiguous()
+        self._flags |= (self._link_bits != 0).to(torch.uint8) * _lib.FLAG_LINKS
+        d.link_bits = self._link_bits.data_ptr()
+        forcing = [b for b in psb if b.calc_force]
+        if forcing:
+            self._force_links = forcing[0].force_links()
+            d.force_links = self._force_links.data_ptr() if len(self._force_links) else None
+            d.n_force_links = len(self._force_links)
+            d.force_out = forcing[0]._force.data_ptr()
+
+    def _choose_pull_post(self):
+        if self._link_bits is not None:
+            self._pull_post = True  # the bounce is part of the pull
+            return
+        super()._choose_pull_post()

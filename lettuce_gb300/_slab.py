@@ -163,6 +163,8 @@ class SlabSimulation:
             if isinstance(nat, NativeBoundary) and nat.kind in (_lib.SUB_ANTI_BOUNCE_BACK,
                                                                 _lib.SUB_EQUILIBRIUM_OUTLET_P):
                 raise ValueError("outlet planes are not decomposed into slabs")
+        if getattr(sim, "_link_bits", None) is not None:
+            raise ValueError("halfway bounce-back links are not decomposed into slabs")
         if _lib.PUSH in sim._patterns and sim._nsb is not None:
             raise ValueError("push steps with populations that do not stream are "
                              "not decomposed into slabs")

@@ -407,6 +407,60 @@ cudaError_t launch_convert(int src_st, const void *src, int dst_st, void *dst, u
     return cudaErrorInvalidValue;
 }
 
+// Momentum exchange of halfway bounce-back links
+// (halfway_bounce_back_boundary.py:211-218): F = 2 sum_k f*_{q_k}(n_k) e_{q_k}
+// over the (q_k, n_k) pairs, read from the post-collision field. One block,
+// a fixed summation order: the result does not depend on scheduling.
+// Entries outside the field are skipped.
+template <int SID, int ST>
+__global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t n_cells,
+                                                         const uint32_t *links, int64_t n_links,
+                                                         double *out) {
+    using S = lgb::Stencil<SID>;
+    using Sto = lgb::Storage<ST>;
+    __shared__ double part[3][256];
+    double F[3] = {0.0, 0.0, 0.0};
+    for (int64_t k = threadIdx.x; k < n_links; k += blockDim.x) {
+        const uint32_t q = links[2 * k], n = links[2 * k + 1];
+        if (q >= (uint32_t)S::Q || (uint64_t)n >= n_cells) continue;
+        double w = 0.0;
+        int e[3] = {0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < S::Q; ++i) {
+            if ((uint32_t)i == q) {
+                w = S::w(i);
+#pragma unroll
+                for (int d = 0; d < S::D; ++d) e[d] = S::e(i, d);
+            }
+        }
+        const double v = (double)Sto::load_plain(
+            static_cast<const typename Sto::T *>(f) + (uint64_t)q * n_cells + n, w);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) F[d] += 2.0 * v * (double)e[d];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) part[d][threadIdx.x] = F[d];
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) part[d][threadIdx.x] += part[d][threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) out[d] = part[d][0];
+    }
+}
+
+template <int SID, int ST>
+cudaError_t launch_link_force_ss(const void *f, uint64_t n_cells, const uint32_t *links,
+                                 int64_t n_links, double *out, cudaStream_t s) {
+    link_force_kernel<SID, ST><<<1, 256, 0, s>>>(f, n_cells, links, n_links, out);
+    return cudaGetLastError();
+}
+
 // stencil x storage switch for the templated helpers above
 #define LGB_SWITCH_SS(stencil, storage, CALL)                                        \
     switch (stencil) {                                                               \
@@ -416,6 +470,15 @@ cudaError_t launch_convert(int src_st, const void *src, int dst_st, void *dst, u
     case LGB_D3Q19: switch (storage) { case 0: return CALL(LGB_D3Q19, 0); case 1: return CALL(LGB_D3Q19, 1); case 2: return CALL(LGB_D3Q19, 2); case 3: return CALL(LGB_D3Q19, 3); } break; \
     case LGB_D3Q27: switch (storage) { case 0: return CALL(LGB_D3Q27, 0); case 1: return CALL(LGB_D3Q27, 1); case 2: return CALL(LGB_D3Q27, 2); case 3: return CALL(LGB_D3Q27, 3); } break; \
     }
+
+cudaError_t launch_link_force(int stencil, int storage, const void *f, uint64_t n_cells,
+                              const uint32_t *links, int64_t n_links, double *out,
+                              cudaStream_t s) {
+#define CALL(SID, ST) launch_link_force_ss<SID, ST>(f, n_cells, links, n_links, out, s)
+    LGB_SWITCH_SS(stencil, storage, CALL)
+#undef CALL
+    return cudaErrorInvalidValue;
+}
 
 cudaError_t moments_dispatch(int stencil, int storage, const Grid &g, const void *f, int aa,
                              void *rho, void *u, cudaStream_t s) {
@@ -585,6 +648,20 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (p.abb_k >= 0 && d->f_in == d->f_out)
         return fail("lgb_step: the anti-bounce-back outlet reads its neighbour plane and "
                     "needs distinct input and output fields");
+    if (d->link_bits) {
+        if (!masked) return fail("lgb_step: bounce-back links need the flag field");
+        if (d->pattern != LGB_PULL && d->pattern != LGB_STREAM_ONLY && d->pattern != LGB_LOCAL)
+            return fail("lgb_step: bounce-back links are applied by pulling streams "
+                        "(LGB_PULL, LGB_STREAM_ONLY) and ignored by LGB_LOCAL; pattern %d",
+                        d->pattern);
+        p.links = d->link_bits;
+    } else if (d->force_links || d->force_out) {
+        return fail("lgb_step: force_links / force_out without link_bits");
+    }
+    if (d->force_out && (d->n_force_links < 0 || (d->n_force_links > 0 && !d->force_links)))
+        return fail("lgb_step: %lld force links at %p", (long long)d->n_force_links,
+                    (const void *)d->force_links);
+    const bool streams = d->pattern == LGB_PULL || d->pattern == LGB_STREAM_ONLY;
     // the kernel variant: BGK with a force is its own collision kind; the
     // patterns without a collision (stream only, AA unpack) run as such
     // whatever the descriptor's collision
@@ -600,6 +677,12 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
                         : dispatch_step(d->stencil, d->storage, coll, d->pattern, masked,
                                         p, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "lgb_step: launch failed");
+    if (d->force_out && streams) {
+        // f_in still holds the post-collision field the links bounced
+        e = launch_link_force(d->stencil, d->storage, d->f_in, g.N, d->force_links,
+                              d->n_force_links, d->force_out, static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return cuda_fail(e, "lgb_step: link force launch failed");
+    }
     return 0;
 }
 

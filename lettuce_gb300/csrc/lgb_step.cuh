@@ -62,6 +62,7 @@ struct StepParams {
     CollideParams cp;
     const uint8_t *flags;
     const uint32_t *nsb;
+    const uint32_t *links;       // halfway bounce-back link bits, or null
     int32_t has_nsm;
     int32_t push_guard;  // the flags carry LGB_FLAG_PUSH_GUARD
     int32_t n_sub;
@@ -110,11 +111,13 @@ template <> struct PatternTraits<LGB_AA_UNPACK> { static constexpr int load = LO
 template <class S, class Sto, int LOAD, bool MASKED, bool RAW = false>
 __device__ __forceinline__ void load_cell(const StepParams &p, const typename Sto::T *__restrict__ fin,
                                           const Nbr &c, uint32_t n, uint32_t nsbits,
-                                          typename Sto::R (&f)[S::Q]) {
+                                          typename Sto::R (&f)[S::Q], uint32_t lbits = 0) {
     const size_t N = p.N;
     // a pull with no-streaming bits keeps the cell's own value for those
-    // populations; cells without any (nearly all) skip the per-population test
-    const bool keep_own = MASKED && LOAD == LOAD_PULL && nsbits != 0;
+    // populations, and a halfway bounce-back link takes the cell's own
+    // opposite population; cells without either (nearly all) skip the
+    // per-population test
+    const bool keep_own = MASKED && LOAD == LOAD_PULL && (nsbits | lbits) != 0;
     auto load_all = [&](const bool check) {
 #pragma unroll
         for (int q = 0; q < S::Q; ++q) {
@@ -123,7 +126,13 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
             if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
                 src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
                 if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
-                if (check && q != 0 && ((nsbits >> q) & 1u)) src = n;
+                if (check && q != 0) {
+                    // the bounce follows the stream (halfway_bounce_back_boundary.py:
+                    // 182-190 runs after ebb_simulation.py:76), so a link wins
+                    // over a no-streaming bit
+                    if ((lbits >> q) & 1u) { src = n; slot = S::opp(q); }
+                    else if ((nsbits >> q) & 1u) src = n;
+                }
             }
             if constexpr (RAW) f[q] = Sto::load_h(fin + (size_t)slot * N + src);
             else f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
@@ -226,8 +235,9 @@ __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename
     const uint32_t nn = (xn * p.Y + yn) * p.Z + zn;
     const uint8_t fl = p.flags[nn];
     const uint32_t nsb = ((fl & LGB_FLAG_NO_STREAM) && p.nsb) ? p.nsb[nn] : 0u;
+    const uint32_t lb = (LOAD == LOAD_PULL && (fl & LGB_FLAG_LINKS) && p.links) ? p.links[nn] : 0u;
     R g[S::Q];
-    load_cell<S, Sto, LOAD, MASKED>(p, fin, cn, nn, nsb, g);
+    load_cell<S, Sto, LOAD, MASKED>(p, fin, cn, nn, nsb, g, lb);
     const int idx = fl & LGB_FLAG_INDEX_MASK;
     if (idx < p.abb_k) apply_local_substep<S, COLL>(p, select_sub(p, idx), cn, g, tab);
     R rho, u[3], rn, un[3];
@@ -309,13 +319,14 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     }
 
     uint8_t fl = 0;
-    uint32_t nsbits = 0;
+    uint32_t nsbits = 0, lbits = 0;
     if (MASKED) {
         fl = p.flags[n];
         if ((fl & LGB_FLAG_NO_STREAM) && p.nsb) nsbits = p.nsb[n];
+        if (LOAD == LOAD_PULL && (fl & LGB_FLAG_LINKS) && p.links) lbits = p.links[n];
     }
     R f[S::Q];
-    load_cell<S, Sto, LOAD, MASKED, HSPACE>(p, fin, c, n, nsbits, f);
+    load_cell<S, Sto, LOAD, MASKED, HSPACE>(p, fin, c, n, nsbits, f, lbits);
 
     if constexpr (HSPACE) {
         if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK)

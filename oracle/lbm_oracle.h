@@ -27,6 +27,10 @@
  *   pressure outlet lettuce/ext/_boundary/equilibrium_outlet_p.py:61-71
  *   partially saturated cells
  *                   lettuce/ext/_boundary/partially_saturated_boundary.py:24-41
+ *   halfway bounce-back (lettuce's example project)
+ *                   examples/advanced_projects/efficient_bounce_back_obstacle/
+ *                   boundary/halfway_bounce_back_boundary.py:170-242 and
+ *                   simulation/ebb_simulation.py:72-101
  *
  * Parity of this restatement with lettuce itself is pinned by golden
  * vectors generated from lettuce (tests/golden/make_golden.py).
@@ -93,6 +97,16 @@ typedef struct {
     double smagorinsky_constant;
     int32_t mrt_equilibrium;
     const double *mrt_tables; /* M [Q][Q], M^-1 [Q][Q], relaxation times [Q] */
+    /* halfway bounce-back links. With n_links > 0 every step runs in the
+     * order of the example EbbSimulation (collide, stream, post-streaming
+     * boundaries) whatever `strategy` says: link k sets population
+     * opp(q_k) of fluid cell n_k, after the stream, to the value that
+     * cell's population q_k had after the collision (q_k points from the
+     * fluid cell into the solid). The momentum-exchange force of step s,
+     * 2 sum_k f*_{q_k}(n_k) e_{q_k}, goes to force_out[3 s .. 3 s + 2]. */
+    int64_t n_links;
+    const int64_t *links;     /* [n_links][2]: q_k, flat cell index n_k */
+    double *force_out;        /* [nsteps][3] or NULL */
 } orc_problem;
 
 int orc_stencil_dq(int stencil, int *d, int *q);

@@ -502,6 +502,33 @@ static int SFX(orc_run_impl)(const orc_problem *p, REAL *f, REAL *work, int nste
     if (nthreads < 1) nthreads = 1;
     const size_t bytes = (size_t)g.q * (size_t)g.N * sizeof(REAL);
     REAL *cur = f, *nxt = work;
+    if (p->n_links > 0) {
+        /* halfway bounce-back (examples/advanced_projects/
+         * efficient_bounce_back_obstacle/boundary/halfway_bounce_back_boundary.py:
+         * __call__ :170-190, calc_force_on_boundary :211-218, store_f_collided
+         * :220-242) in the EbbSimulation order (simulation/ebb_simulation.py:72-76,
+         * 93-101) */
+        REAL *fcol = (REAL *)malloc((size_t)p->n_links * sizeof(REAL));
+        if (!fcol) return -3;
+        for (int s = 0; s < nsteps; ++s) {
+            SFX(collide)(&g, p, cur, nthreads);
+            for (int64_t k = 0; k < p->n_links; ++k)
+                fcol[k] = cur[p->links[2 * k] * g.N + p->links[2 * k + 1]];
+            SFX(stream)(&g, p, cur, nxt, nthreads);
+            { REAL *t = cur; cur = nxt; nxt = t; }
+            double force[3] = {0.0, 0.0, 0.0};
+            for (int64_t k = 0; k < p->n_links; ++k) {
+                const int q = (int)p->links[2 * k];
+                cur[(int64_t)g.st->opp[q] * g.N + p->links[2 * k + 1]] = fcol[k];
+                for (int d = 0; d < g.d; ++d) force[d] += 2.0 * (double)fcol[k] * g.st->e[q][d];
+            }
+            if (p->force_out)
+                for (int d = 0; d < 3; ++d) p->force_out[3 * s + d] = force[d];
+        }
+        free(fcol);
+        if (cur != f) memcpy(f, cur, bytes);
+        return 0;
+    }
     for (int s = 0; s < nsteps; ++s) {
         const int pre = (p->strategy & ORC_PRE_STREAMING) != 0;
         const int post = (p->strategy & ORC_POST_STREAMING) != 0;

@@ -108,7 +108,10 @@ class _Problem(ctypes.Structure):
                 ("accel", ctypes.c_double * 3),
                 ("smagorinsky_constant", ctypes.c_double),
                 ("mrt_equilibrium", ctypes.c_int32),
-                ("mrt_tables", ctypes.c_void_p)]
+                ("mrt_tables", ctypes.c_void_p),
+                ("n_links", ctypes.c_int64),
+                ("links", ctypes.c_void_p),
+                ("force_out", ctypes.c_void_p)]
 
 
 def build():
@@ -209,15 +212,52 @@ def assemble_masks(resolution, q, name, pre, post):
     return ncm, nsm
 
 
+def ebb_masks(resolution, q, name, pre, post, post_streaming):
+    """the masks of the example EbbSimulation
+    (examples/advanced_projects/efficient_bounce_back_obstacle/simulation/
+    ebb_simulation.py:28-57): lettuce's masks, created filled with the
+    collision index if there were none, then each post-streaming
+    boundary's solid cells take index collision_index + 1 + len(post) + j
+    and keep all populations in the stream"""
+    ncm, nsm = assemble_masks(resolution, q, name, pre, post)
+    if not post_streaming:
+        return ncm, nsm
+    ci = len(pre)
+    if ncm is None:
+        ncm = np.full(list(resolution), ci, dtype=np.uint8)
+        nsm = np.full([q] + list(resolution), ci, dtype=np.uint8)
+    for i, b in enumerate(post_streaming, start=ci + 1 + len(post)):
+        solid = np.asarray(b["solid"], dtype=bool)
+        ncm[solid] = i
+        nsm |= solid[None].astype(np.uint8)
+    return ncm, nsm
+
+
+def link_cells(f_index, resolution):
+    """(q, flat cell index) rows of a halfway bounce-back link list given as
+    (q, x, y[, z]) rows; negative coordinates count from the end, as the
+    example's torch indexing reads them"""
+    fi = np.asarray(f_index, dtype=np.int64).reshape(-1, len(resolution) + 1)
+    res = np.array(resolution, dtype=np.int64)
+    cells = np.where(fi[:, 1:] < 0, fi[:, 1:] + res, fi[:, 1:])
+    flat = np.ravel_multi_index(tuple(cells.T), tuple(resolution))
+    return np.ascontiguousarray(np.stack([fi[:, 0], flat], axis=1).astype(np.int64))
+
+
 def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
         strategy="POST_STREAMING", pre=(), post=(), nthreads=None,
         masks=None, force=None, force_tau=1.0, accel=(0.0, 0.0, 0.0),
-        smagorinsky_constant=0.17, mrt=None):
+        smagorinsky_constant=0.17, mrt=None, post_streaming=(), forces=None):
     """Advance ``f`` ([Q, *res], float64 or float32) by ``nsteps`` steps and
     return the new array; ``f`` is not modified. ``force`` ("guo",
     "shan_chen" or None) with ``force_tau`` and ``accel`` (lattice units)
     applies to the BGK and Smagorinsky collisions. ``mrt`` = (equilibrium
-    name, M, M^-1, relaxation times) for the "mrt" collision."""
+    name, M, M^-1, relaxation times) for the "mrt" collision.
+    ``post_streaming``: halfway bounce-back boundaries, dicts with "solid"
+    (mask) and "f_index" (link rows q, x, y[, z]); with any, every step runs
+    collide, stream, bounce (the example EbbSimulation) whatever
+    ``strategy`` says, and ``forces`` (float64 [nsteps, 3], optional)
+    receives each step's momentum-exchange force over all links."""
     L = lib()
     f = np.ascontiguousarray(f)
     dt = f.dtype
@@ -225,8 +265,9 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
     q = f.shape[0]
     res = list(f.shape[1:])
     pre, post = list(pre), list(post)
+    post_streaming = list(post_streaming)
     if masks is None:
-        ncm, nsm = assemble_masks(res, q, name, pre, post)
+        ncm, nsm = ebb_masks(res, q, name, pre, post, post_streaming)
     else:
         ncm, nsm = masks
     keep = []
@@ -288,6 +329,15 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
     p.n_sub = len(pre) + 1 + len(post)
     p.collision_index = len(pre)
     p.sub = subs
+    if post_streaming:
+        links = np.concatenate([link_cells(b["f_index"], res) for b in post_streaming], axis=0)
+        keep.append(links)
+        p.n_links = len(links)
+        p.links = links.ctypes.data
+        if forces is not None:
+            assert forces.dtype == np.float64 and forces.shape == (nsteps, 3)
+            assert forces.flags["C_CONTIGUOUS"]
+            p.force_out = forces.ctypes.data
     out = f.copy()
     work = np.empty_like(f)
     nthreads = nthreads or os.cpu_count() or 1

@@ -438,8 +438,111 @@ def case_dump():
                         meta=json.dumps({"res": [12, 12], "re": 100, "ma": 0.05}))
 
 
+EBB = os.path.join("examples", "advanced_projects", "efficient_bounce_back_obstacle")
+
+
+def case_hwbb(name, stencil, res, coll, steps, seed, solid, periodicity=None,
+              inlet=False, global_extra=None):
+    """lettuce's example halfway bounce-back boundary
+    (examples/advanced_projects/efficient_bounce_back_obstacle/boundary/
+    halfway_bounce_back_boundary.py) under the example's EbbSimulation
+    (simulation/ebb_simulation.py: collide, stream, then the post-streaming
+    boundaries), with its momentum-exchange force after every step. The
+    link list comes from the boundary's own neighbour search (no solid
+    boundary data given). ``inlet`` adds an equilibrium boundary on the x = 0
+    plane as an ordinary post-collision boundary; ``global_extra`` is a
+    second solid region given as part of ``global_solid_mask``."""
+    import lettuce
+    root = os.path.dirname(os.path.dirname(os.path.abspath(lettuce.__file__)))
+    for sub in ("boundary", "simulation"):
+        d = os.path.join(root, EBB, sub)
+        if d not in sys.path:
+            sys.path.insert(0, d)
+    from halfway_bounce_back_boundary import HalfwayBounceBackBoundary
+    from solid_boundary_data import SolidBoundaryData
+    from ebb_simulation import EbbSimulation
+
+    class HwbbFlow(GivenFlow):
+        psb = []
+
+        @property
+        def post_streaming_boundaries(self):
+            return self.psb
+
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.2 * rng.standard_normal([st.q] + res))
+    flow = HwbbFlow(st, f0)
+    if inlet:
+        m = np.zeros(res, dtype=bool)
+        m[0] = True
+        flow.bnds = [EquilibriumBoundaryPU(CTX, flow, torch.tensor(m),
+                                           torch.tensor([0.02] + [0.0] * (len(res) - 1),
+                                                        dtype=torch.float64))]
+    # the example's neighbour search sizes its periodic-border offsets by
+    # flow.context.d, an attribute lettuce's Context does not have: give it
+    flow.context.d = st.d
+    sbd = SolidBoundaryData()
+    sbd.solid_mask = solid
+    gmask = None if global_extra is None else (solid | global_extra)
+    hw = HalfwayBounceBackBoundary(CTX, flow, sbd, global_solid_mask=gmask,
+                                   periodicity=periodicity, calc_force=True)
+    flow.psb = [hw]
+    tau = 0.8
+    sim = EbbSimulation(flow, collision_of(coll, tau), [])
+    out = {"f0": f0, "solid": solid, "tau": np.float64(tau), "steps": np.int64(steps),
+           "f_index": npf(hw.f_index).astype(np.int64),
+           "ncm": npf(sim.no_collision_mask).astype(np.uint8),
+           "nsm": npf(sim.no_streaming_mask).astype(np.uint8)}
+    if global_extra is not None:
+        out["global_extra"] = global_extra
+    if inlet:
+        b = flow.bnds[0]
+        out["inlet_u_lu"] = npf(flow.units.convert_velocity_to_lu(b.velocity))
+        out["inlet_rho_lu"] = npf(flow.units.convert_pressure_pu_to_density_lu(b.pressure))
+    forces = []
+    for _ in range(steps):
+        sim(1)
+        forces.append(npf(hw.force_sum))
+    out["force"] = np.array(forces)
+    out["f"] = npf(flow.f)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res, "collision": coll,
+                              "periodicity": None if periodicity is None else list(periodicity),
+                              "inlet": bool(inlet)})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def hwbb_cases():
+    # a disc inside a non-periodic 2-D box, and two blocks on the x = 0 and
+    # x = 23 columns: the neighbour search wraps negative indices (Python
+    # indexing) and drops those past the end
+    g = np.meshgrid(np.arange(24), np.arange(14), indexing="ij")
+    solid = (g[0] - 10.0) ** 2 + (g[1] - 6.5) ** 2 < 3.2 ** 2
+    solid[0, 3:6] = True
+    solid[23, 8:10] = True
+    case_hwbb("hwbb_d2q9_bgk", D2Q9, [24, 14], "bgk", 6, 80, solid)
+    # a sphere, periodic along z, behind an equilibrium inlet (mask index of
+    # the post-streaming boundary after the ordinary boundaries)
+    g = np.meshgrid(np.arange(12), np.arange(8), np.arange(6), indexing="ij")
+    solid = (g[0] - 5.0) ** 2 + (g[1] - 3.5) ** 2 + (g[2] - 2.5) ** 2 < 2.2 ** 2
+    case_hwbb("hwbb_d3q19_trt", D3Q19, [12, 8, 6], "trt", 4, 81, solid,
+              periodicity=(False, False, True), inlet=True)
+    # a cube touching y = 0 with y periodic, next to a second solid region
+    # given only through global_solid_mask
+    solid = np.zeros([8, 6, 5], dtype=bool)
+    solid[2:5, 0:2, 1:4] = True
+    extra = np.zeros_like(solid)
+    extra[5:7, 0:2, 1:3] = True
+    case_hwbb("hwbb_d3q27_bgk", D3Q27, [8, 6, 5], "bgk", 3, 82, solid,
+              periodicity=(True, True, False), global_extra=extra)
+
+
 def main():
     torch.set_num_threads(os.cpu_count() or 1)
+    if "--only-hwbb" in sys.argv:
+        hwbb_cases()
+        return
     case_tgv("tgv2d_d2q9_bgk", D2Q9, 16, 1000, "bgk", 5)
     case_tgv("tgv2d_d2q9_trt", D2Q9, [16, 12], 300, "trt", 5)
     case_tgv("tgv2d_d2q9_kbc", D2Q9, 16, 1000, "kbc", 5)
@@ -475,6 +578,7 @@ def main():
     case_poiseuille("poiseuille_guo", "guo", 300)
     case_poiseuille("poiseuille_shanchen", "shan_chen", 300)
     case_dump()
+    hwbb_cases()
     case_native_kats()
     case_observables()
     case_adjoint()

@@ -76,3 +76,37 @@ def obstacle_oracle_boundaries(z, m):
              "u": z["inlet_u_lu"].reshape([d] + [1] * d)},
             {"kind": "anti_bounce_back", "direction": [1] + [0] * (d - 1)},
             {"kind": "bounce_back", "mask": z["mask"]}]
+
+
+class HwbbFlow(GivenFlow):
+    """a given-populations flow with post-streaming boundaries (the
+    property the example EbbSimulation looks for on the flow's class)"""
+    psb = ()
+
+    @property
+    def post_streaming_boundaries(self):
+        return list(self.psb)
+
+
+def hwbb_case(context, z, meta, f0=None):
+    """(flow, boundary) of a halfway bounce-back golden case: the given
+    populations, the optional equilibrium inlet on x = 0 and the boundary
+    with its force computed"""
+    stencil = getattr(lt, meta["stencil"])()
+    f0 = z["f0"] if f0 is None else f0
+    flow = HwbbFlow(context, stencil, f0)
+    res = list(meta["res"])
+    if meta["inlet"]:
+        m = torch.zeros(res, dtype=torch.bool)
+        m[0] = True
+        vel = torch.tensor([0.02] + [0.0] * (len(res) - 1), dtype=context.dtype)
+        flow._bnds = [lt.EquilibriumBoundaryPU(context, flow, m, vel)]
+    sbd = lt.SolidBoundaryData()
+    sbd.solid_mask = z["solid"]
+    g = None if "global_extra" not in z else (z["solid"] | z["global_extra"])
+    per = meta["periodicity"]
+    hw = lt.HalfwayBounceBackBoundary(context, flow, sbd, global_solid_mask=g,
+                                      periodicity=None if per is None else tuple(per),
+                                      calc_force=True)
+    flow.psb = [hw]
+    return flow, hw

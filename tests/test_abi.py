@@ -36,10 +36,12 @@ def test_struct_layout_matches_header(tmp_path, lgb):
     src = tmp_path / "probe.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "lettuce_gb300.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(lgb_step_desc),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\","
+        " sizeof(lgb_step_desc),"
         " offsetof(lgb_step_desc, sub), offsetof(lgb_step_desc, options),"
         " sizeof(lgb_substep), offsetof(lgb_substep, rho), offsetof(lgb_substep, u_stride),"
-        " offsetof(lgb_step_desc, accel), offsetof(lgb_step_desc, smagorinsky_constant));"
+        " offsetof(lgb_step_desc, accel), offsetof(lgb_step_desc, smagorinsky_constant),"
+        " offsetof(lgb_step_desc, link_bits), offsetof(lgb_step_desc, force_out));"
         "return 0;}\n")
     exe = tmp_path / "probe"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)],
@@ -49,7 +51,7 @@ def test_struct_layout_matches_header(tmp_path, lgb):
     S, D = _lib.Substep, _lib.StepDesc
     assert got == [ctypes.sizeof(D), D.sub.offset, D.options.offset, ctypes.sizeof(S),
                    S.rho.offset, S.u_stride.offset, D.accel.offset,
-                   D.smagorinsky_constant.offset]
+                   D.smagorinsky_constant.offset, D.link_bits.offset, D.force_out.offset]
 
 
 def _desc(**kw):
@@ -113,6 +115,21 @@ def test_step_validation_masked(lgb):
     d.sub[1].kind = _lib.SUB_BOUNCE_BACK
     assert L.lgb_step(ctypes.byref(d), None) != 0
     assert "collision_index" in L.lgb_last_error().decode()
+    # halfway bounce-back links: pulling patterns only, with flags; a force
+    # output only with links (all rejected before any device call)
+    for kw, msg in [(dict(link_bits=0x5000), "need the flag field"),
+                    (dict(flags=0x3000, n_sub=1, collision_index=0, link_bits=0x5000,
+                          pattern=_lib.PUSH), "pulling streams"),
+                    (dict(flags=0x3000, n_sub=1, collision_index=0, link_bits=0x5000,
+                          pattern=_lib.AA_EVEN, f_out=0x1000), "pulling streams"),
+                    (dict(force_out=0x6000), "without link_bits"),
+                    (dict(force_links=0x6000), "without link_bits"),
+                    (dict(flags=0x3000, n_sub=1, collision_index=0, link_bits=0x5000,
+                          force_out=0x6000, n_force_links=4), "force links")]:
+        d = _desc(**kw)
+        d.sub[0].kind = _lib.SUB_COLLISION
+        assert L.lgb_step(ctypes.byref(d), None) != 0
+        assert msg in L.lgb_last_error().decode()
 
 
 def test_reduce_and_convert_validation(lgb):

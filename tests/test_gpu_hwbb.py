@@ -1,0 +1,118 @@
+"""Halfway bounce-back (the post-streaming boundary of lettuce's example
+project, run by ``EbbSimulation``) through the step kernel's pull: the
+populations after every step and the momentum-exchange force of each step
+against the golden vectors of the example itself (float64), against the
+oracle in float32 and 16-bit storage, graph replay against eager steps, and
+a reporter that reads the force while the stream is pending."""
+import numpy as np
+import pytest
+import torch
+
+import lettuce_gb300 as lt
+from conftest import golden, golden_names, meta
+from lgb_helpers import hwbb_case, rel_max, to_np
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_names("hwbb_")
+
+
+def _sim(z, m, dtype=torch.float64, storage=None, use_graph=False, f0=None):
+    ctx = lt.Context("cuda:0", dtype, storage=storage)
+    flow, hw = hwbb_case(ctx, z, m, f0=f0)
+    coll = lt.TRTCollision(float(z["tau"]), 1.0) if m["collision"] == "trt" else \
+        lt.BGKCollision(float(z["tau"]))
+    return lt.EbbSimulation(flow, coll, [], use_graph=use_graph), flow, hw
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_f64_matches_example_step_by_step(lgb, name):
+    z = golden(name)
+    m = meta(z)
+    sim, flow, hw = _sim(z, m)
+    forces = []
+    for _ in range(int(z["steps"])):
+        sim(1)
+        forces.append(to_np(hw.force_sum))
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(np.array(forces), z["force"], rtol=0, atol=1e-12)
+    assert sim.status == 0
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_f64_graph_run_matches_example(lgb, name):
+    """all steps in one call (collide-only launch, pull launches from a
+    captured graph, the last stream pending until read)"""
+    z = golden(name)
+    m = meta(z)
+    sim, flow, hw = _sim(z, m, use_graph=True)
+    sim(int(z["steps"]))
+    assert flow._stream_pending is not None
+    np.testing.assert_allclose(to_np(hw.force_sum), z["force"][-1], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("storage,tol", [(None, 2e-6), ("fp16_shifted", 2e-3),
+                                         ("bf16_shifted", 1.5e-2)])
+def test_reduced_precision_against_oracle(lgb, oracle, storage, tol):
+    z = golden("hwbb_d3q19_trt")
+    m = meta(z)
+    steps = 12
+    forces = np.zeros((steps, 3))
+    from test_hwbb_cpu import _post
+    ref = oracle.run(m["stencil"], z["f0"].astype(np.float32), steps, collision="trt",
+                     tau=float(z["tau"]), tau_minus=1.0, post=_post(z, m),
+                     post_streaming=[dict(solid=z["solid"], f_index=z["f_index"])],
+                     forces=forces)
+    sim, flow, hw = _sim(z, m, torch.float32, storage, use_graph=True,
+                         f0=z["f0"].astype(np.float32))
+    sim(steps)
+    assert rel_max(to_np(flow.f), ref) < tol
+    assert rel_max(to_np(hw.force_sum), forces[-1]) < 20 * tol
+
+
+def test_eager_and_graph_runs_identical(lgb):
+    z = golden("hwbb_d3q27_bgk")
+    m = meta(z)
+    a, fa, ha = _sim(z, m, torch.float32, use_graph=False, f0=z["f0"].astype(np.float32))
+    b, fb, hb = _sim(z, m, torch.float32, use_graph=True, f0=z["f0"].astype(np.float32))
+    a(11)
+    b(11)
+    assert torch.equal(fa.f, fb.f)
+    assert torch.equal(ha.force_sum, hb.force_sum)
+
+
+def test_force_reporter_reads_each_step(lgb):
+    """a reporter reading the force every 3 steps sees the example's force of
+    that step (the read applies the pending stream and bounce)"""
+    z = golden("hwbb_d2q9_bgk")
+    m = meta(z)
+    seen = {}
+
+    class ForceReporter(lt.Reporter):
+        def __call__(self, simulation):
+            if simulation.flow.i % self.interval == 0 and simulation.flow.i > 0:
+                seen[simulation.flow.i] = to_np(hw.force_sum)
+
+    ctx = lt.Context("cuda:0", torch.float64)
+    flow, hw = hwbb_case(ctx, z, m)
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(float(z["tau"])), [ForceReporter(3)],
+                           use_graph=True)
+    sim(6)
+    assert sorted(seen) == [3, 6]
+    for i, F in seen.items():
+        np.testing.assert_allclose(F, z["force"][i - 1], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+
+
+def test_stream_half_alone_bounces(lgb):
+    """lettuce's collide and stream halves called directly reproduce the
+    step (the stream half carries the bounce)"""
+    z = golden("hwbb_d2q9_bgk")
+    m = meta(z)
+    sim, flow, hw = _sim(z, m)
+    for _ in range(int(z["steps"])):
+        sim._collide()
+        sim._stream()
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(to_np(hw.force_sum), z["force"][-1], rtol=0, atol=1e-12)

@@ -1,0 +1,127 @@
+"""Halfway bounce-back of lettuce's example project (the post-streaming
+boundary of examples/advanced_projects/efficient_bounce_back_obstacle), on
+CPU: the oracle against the golden vectors the example itself produced
+(populations after every step's collide, stream, bounce, and the
+momentum-exchange force of each step), the product's neighbour search
+against the example's link lists, and the masks, link bits and force links
+``EbbSimulation`` builds on a CPU context (set-up only)."""
+import numpy as np
+import pytest
+import torch
+
+import lettuce_gb300 as lt
+from conftest import golden, golden_names, meta
+from lgb_helpers import hwbb_case
+
+CASES = golden_names("hwbb_")
+
+
+def _post(z, m):
+    if not m["inlet"]:
+        return []
+    res = list(m["res"])
+    mask = np.zeros(res, dtype=bool)
+    mask[0] = True
+    return [dict(kind="equilibrium_pu", mask=mask, rho=z["inlet_rho_lu"], u=z["inlet_u_lu"])]
+
+
+def test_cases_present():
+    assert len(CASES) == 3
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_example(oracle, name):
+    z = golden(name)
+    m = meta(z)
+    steps = int(z["steps"])
+    forces = np.zeros((steps, 3))
+    out = oracle.run(m["stencil"], z["f0"], steps, collision=m["collision"],
+                     tau=float(z["tau"]), tau_minus=1.0, post=_post(z, m),
+                     post_streaming=[dict(solid=z["solid"], f_index=z["f_index"])],
+                     forces=forces)
+    np.testing.assert_allclose(out, z["f"], rtol=0, atol=1e-14)
+    d = len(m["res"])
+    np.testing.assert_allclose(forces[:, :d], z["force"], rtol=0, atol=1e-13)
+    assert np.all(forces[:, d:] == 0)
+    ncm, nsm = oracle.ebb_masks(list(m["res"]), z["f0"].shape[0], m["stencil"], [],
+                                _post(z, m), [dict(solid=z["solid"])])
+    assert np.array_equal(ncm, z["ncm"]) and np.array_equal(nsm, z["nsm"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_neighbour_search_matches_example(name):
+    """same rows in the same order, negative coordinates kept as the
+    example writes them (the non-periodic wrap of Python indexing)"""
+    z = golden(name)
+    m = meta(z)
+    st = getattr(lt, m["stencil"])()
+    per = m["periodicity"]
+    g = None if "global_extra" not in z else (z["solid"] | z["global_extra"])
+    rows = lt.hwbb_links(st.e, st.opposite, z["solid"], g,
+                         None if per is None else tuple(per)[:st.d])
+    assert rows.dtype == np.int64
+    assert np.array_equal(rows, z["f_index"])
+
+
+def test_given_link_lists_take_precedence():
+    z = golden("hwbb_d2q9_bgk")
+    m = meta(z)
+    flow, hw = hwbb_case(lt.Context("cpu", torch.float64), z, m)
+    sbd = lt.SolidBoundaryData()
+    sbd.solid_mask = z["solid"]
+    sbd.f_index_lt = z["f_index"][:10]
+    sbd.f_index_gt = z["f_index"][10:12]
+    b = lt.HalfwayBounceBackBoundary(flow.context, flow, sbd)
+    assert np.array_equal(b.f_index.numpy(), z["f_index"][:12])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_ebb_masks_and_links_on_cpu(name):
+    z = golden(name)
+    m = meta(z)
+    flow, hw = hwbb_case(lt.Context("cpu", torch.float64), z, m)
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.8), [])
+    assert np.array_equal(sim.no_collision_mask.numpy(), z["ncm"])
+    assert np.array_equal(sim.no_streaming_mask.numpy(), z["nsm"])
+    # link bits: bit opp(q) at the fluid cell of every link (q, x)
+    bits = sim._link_bits.numpy().view(np.uint32)
+    st = flow.stencil
+    res = np.array(m["res"])
+    want = np.zeros(bits.shape, dtype=np.uint32)
+    for row in z["f_index"]:
+        c = tuple(np.where(row[1:] < 0, row[1:] + res, row[1:]))
+        want[c] |= np.uint32(1 << st.opposite[row[0]])
+    assert np.array_equal(bits, want)
+    flags = sim._flags.numpy()
+    assert np.array_equal((flags & lt._lib.FLAG_LINKS) != 0, want != 0)
+    assert not np.any(z["solid"] & (want != 0))          # links sit on fluid cells
+    assert int(sim._desc.link_bits) == sim._link_bits.data_ptr()
+    pairs = sim._force_links.numpy().view(np.uint32)
+    assert pairs.shape == (len(z["f_index"]), 2)
+    flat = np.ravel_multi_index(tuple(np.where(z["f_index"][:, 1:] < 0,
+                                               z["f_index"][:, 1:] + res,
+                                               z["f_index"][:, 1:]).T), tuple(res))
+    assert np.array_equal(pairs[:, 0], z["f_index"][:, 0]) and np.array_equal(pairs[:, 1], flat)
+    assert sim._pull_post and sim._desc.n_force_links == len(pairs)
+
+
+def test_ebb_rejections_on_cpu():
+    z = golden("hwbb_d2q9_bgk")
+    m = meta(z)
+    flow, hw = hwbb_case(lt.Context("cpu", torch.float64), z, m)
+    with pytest.raises(RuntimeError, match="EbbSimulation"):
+        hw(flow)
+    hw2 = lt.HalfwayBounceBackBoundary(flow.context, flow, type("S", (), {"solid_mask": z["solid"]})(),
+                                       calc_force=True)
+    flow.psb = [hw, hw2]
+    with pytest.raises(NotImplementedError, match="force"):
+        lt.EbbSimulation(flow, lt.BGKCollision(0.8), [])
+    flow.psb = [lt.BounceBackBoundary(torch.as_tensor(z["solid"]))]
+    with pytest.raises(NotImplementedError, match="BounceBackBoundary"):
+        lt.EbbSimulation(flow, lt.BGKCollision(0.8), [])
+    flow.psb = [hw]
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.8), [])
+    with pytest.raises(ValueError, match="slabs"):
+        lt.SlabSimulation(sim, 2)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        sim(1)
