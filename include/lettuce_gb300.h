@@ -146,15 +146,34 @@ typedef struct {
      * pulled from x - e_q (a solid cell) but takes the cell's own
      * post-collision population opp(q). NULL = no links. */
     const uint32_t *link_bits;   /* [N] */
+    /* Interpolated links, the linear interpolated bounce-back of the same
+     * project (boundary/linear_interpolated_bounce_back_boundary.py:55-96).
+     * With link_val set, every linked population takes link_val[k],
+     * k = link_base[n] + (number of link bits below q in link_bits[n]).
+     * LGB_PULL and LGB_STREAM_ONLY launches first fill link_val from f_in
+     * for the n_links links: link_pairs holds (q, n), q pointing from cell
+     * n into the solid, sorted by n and then by opp(q); link_d the wall
+     * distance d (< 0: a halfway link, f*_q(n)); g = f*_q(n):
+     *   d < 1/2:  2 d g + (1 - 2 d) f*_q(n - e_q)
+     *   d >= 1/2: g / (2 d) + (1 - 1 / (2 d)) f*_{opp(q)}(n).
+     * link_val is scratch in the compute type (double for LGB_F64, float
+     * otherwise). NULL link_val: every link is a halfway link. */
+    const uint32_t *link_base;   /* [N] */
+    const uint32_t *link_pairs;  /* [n_links][2] */
+    const double *link_d;        /* [n_links] */
+    void *link_val;              /* [n_links] */
+    int64_t n_links;
     /* Momentum exchange on the links of one boundary
-     * (halfway_bounce_back_boundary.py:211-218): force_links holds
-     * n_force_links pairs (q, n), q pointing from fluid cell n into the
-     * solid. LGB_PULL and LGB_STREAM_ONLY launches, whose stream crosses the
-     * links, write 2 sum f*_q(n) e_q (f* = the post-collision field f_in)
-     * to force_out (float64 [3], lattice units, lettuce dimension order;
-     * unused trailing entries 0); LGB_LOCAL leaves it. Device memory;
-     * NULL / 0 = not computed. */
-    const uint32_t *force_links; /* [n_force_links][2] */
+     * (halfway_bounce_back_boundary.py:211-218,
+     * linear_interpolated_bounce_back_boundary.py:104-126): force_links
+     * holds n_force_links triplets (q, n, k), q pointing from cell n into
+     * the solid, k the link's index in link_val or 0xffffffff for a halfway
+     * link. LGB_PULL and LGB_STREAM_ONLY launches, whose stream crosses the
+     * links, write sum (f*_q(n) + b) e_q, b = link_val[k] or f*_q(n)
+     * (f* = the post-collision field f_in), to force_out (float64 [3],
+     * lattice units, lettuce dimension order; unused trailing entries 0);
+     * LGB_LOCAL leaves it. Device memory; NULL / 0 = not computed. */
+    const uint32_t *force_links; /* [n_force_links][3] */
     int64_t n_force_links;
     double *force_out;
 } lgb_step_desc;

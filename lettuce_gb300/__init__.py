@@ -18,7 +18,8 @@ from ._collision import (BGKCollision, Collision, KBCCollision, MRTCollision, No
 from ._moments import D1Q3Transform, D2Q9Dellar, D2Q9Lallemand, D3Q27Hermite, Transform
 from ._force import Force, Guo, ShanChen
 from ._boundary import (AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU,
-                        EquilibriumOutletP, HalfwayBounceBackBoundary, PartiallySaturatedBC,
+                        EquilibriumOutletP, HalfwayBounceBackBoundary,
+                        LinearInterpolatedBounceBackBoundary, PartiallySaturatedBC,
                         SolidBoundaryData, hwbb_links)
 from ._simulation import (BreakableSimulation, EbbSimulation, Reporter, Simulation,
                           StreamingStrategy)
@@ -39,7 +40,8 @@ __all__ = [
     "initialize_f_neq", "torch_gradient", "Collision", "BGKCollision",
     "TRTCollision", "KBCCollision", "NoCollision", "BounceBackBoundary",
     "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "EquilibriumOutletP",
-    "PartiallySaturatedBC", "HalfwayBounceBackBoundary", "SolidBoundaryData", "hwbb_links",
+    "PartiallySaturatedBC", "HalfwayBounceBackBoundary", "LinearInterpolatedBounceBackBoundary",
+    "SolidBoundaryData", "hwbb_links",
     "Simulation", "EbbSimulation",
     "BreakableSimulation", "StreamingStrategy", "Reporter", "Observable",
     "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",

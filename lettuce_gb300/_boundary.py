@@ -5,10 +5,13 @@
 * AntiBounceBackOutlet -- lettuce/ext/_boundary/anti_bounce_back_outlet.py:13-109
 * EquilibriumOutletP -- lettuce/ext/_boundary/equilibrium_outlet_p.py:12-91
 * PartiallySaturatedBC -- lettuce/ext/_boundary/partially_saturated_boundary.py:6-51
-* HalfwayBounceBackBoundary, SolidBoundaryData -- lettuce's example project
+* HalfwayBounceBackBoundary, LinearInterpolatedBounceBackBoundary,
+  SolidBoundaryData -- lettuce's example project
   examples/advanced_projects/efficient_bounce_back_obstacle/boundary/
-  halfway_bounce_back_boundary.py:10-254 and solid_boundary_data.py:7-14; a
-  post-streaming boundary, run by ``EbbSimulation``
+  halfway_bounce_back_boundary.py:10-254,
+  linear_interpolated_bounce_back_boundary.py:9-212 and
+  solid_boundary_data.py:7-14; post-streaming boundaries, run by
+  ``EbbSimulation``
 
 The masks are built exactly as lettuce builds them (they are combined by
 ``Simulation`` into the per-cell flag byte); the operators themselves run
@@ -29,7 +32,7 @@ from ._native import NativeBoundary, NativeCollision
 
 __all__ = ["BounceBackBoundary", "EquilibriumBoundaryPU", "AntiBounceBackOutlet",
            "EquilibriumOutletP", "PartiallySaturatedBC", "SolidBoundaryData",
-           "HalfwayBounceBackBoundary", "hwbb_links"]
+           "HalfwayBounceBackBoundary", "LinearInterpolatedBounceBackBoundary", "hwbb_links"]
 
 
 def _apply_alone(flow, native: NativeBoundary, flags_value):
@@ -320,29 +323,11 @@ class HalfwayBounceBackBoundary(Boundary):
         self.flow._settle()
         return self._force[:self.flow.stencil.d].to(self.context.dtype)
 
-    def link_bits(self) -> torch.Tensor:
-        """int32 [*res]: bit opp(q) set at fluid cell x for every link
-        (q, x); the pull at x then takes its own population q for opp(q)"""
-        st = self.flow.stencil
-        res = list(self.flow.resolution)
-        fi = self.f_index.detach().cpu().numpy()
-        bits = np.zeros(res, dtype=np.int64)
-        if len(fi):
-            opp = np.asarray(st.opposite, dtype=np.int64)
-            cells = np.where(fi[:, 1:] < 0, fi[:, 1:] + np.array(res), fi[:, 1:])
-            np.bitwise_or.at(bits, tuple(cells.T), np.left_shift(1, opp[fi[:, 0]]))
-        return torch.as_tensor(bits.astype(np.uint32).view(np.int32),
-                               device=self.context.device).contiguous()
-
-    def force_links(self) -> torch.Tensor:
-        """uint32 pairs [n, 2] (q, flat cell index) of the links, as int32
-        (the device list the momentum-exchange kernel reads)"""
-        res = list(self.flow.resolution)
-        fi = self.f_index.detach().cpu().numpy()
-        cells = np.where(fi[:, 1:] < 0, fi[:, 1:] + np.array(res), fi[:, 1:])
-        flat = np.ravel_multi_index(tuple(cells.T), tuple(res)) if len(fi) else np.zeros(0, int)
-        pairs = np.stack([fi[:, 0], flat], axis=1).astype(np.uint32).view(np.int32)
-        return torch.as_tensor(np.ascontiguousarray(pairs), device=self.context.device)
+    def link_rows(self):
+        """(link rows q, x, y[, z] as int64 [K, 1 + D], wall distances
+        float64 [K]: -1, the halfway links)"""
+        rows = self.f_index.detach().cpu().numpy().astype(np.int64)
+        return rows, np.full(len(rows), -1.0)
 
     def __call__(self, flow):
         raise RuntimeError("the halfway bounce-back runs inside the step of an EbbSimulation")
@@ -358,4 +343,78 @@ class HalfwayBounceBackBoundary(Boundary):
 
     def native_generator(self, index: int) -> NativeBoundary:
         # the solid cells run no substep; the links travel as bits
+        return NativeBoundary(_lib.SUB_NONE, index)
+
+
+class LinearInterpolatedBounceBackBoundary(Boundary):
+    """Linear interpolated bounce-back (Bouzidi et al. 2001; the example
+    project's IBB1, linear_interpolated_bounce_back_boundary.py:9-212) with
+    momentum exchange. The links and wall distances come from the solid
+    boundary data: ``f_index_lt`` / ``d_lt`` (d < 1/2) and ``f_index_gt`` /
+    ``d_gt``, rows q, x, y[, z] with q pointing from the fluid cell into the
+    solid. After each step's stream the fluid cell x takes for population
+    opp(q)
+      d < 1/2:  2 d f*_q(x) + (1 - 2 d) f_q(x)   (f_q(x) the streamed value)
+      d >= 1/2: f*_q(x) / (2 d) + (1 - 1 / (2 d)) f*_{opp(q)}(x),
+    f* the post-collision populations. With ``calc_force`` the momentum
+    exchange sum (f*_q(x) + f_opp(q)(x)) e_q over the links is kept as
+    ``force_sum``. The solid cells neither collide nor stream. The
+    interpolation runs as a pass over the links before each pulling step
+    kernel, which reads the bounced values (``EbbSimulation``)."""
+
+    def __init__(self, context, flow, solid_boundary_data, calc_force: bool = False):
+        self.context = context
+        self.flow = flow
+        self.mask = _to_numpy_bool(solid_boundary_data.solid_mask)
+        d1 = flow.stencil.d + 1
+        self.f_index_lt = torch.as_tensor(
+            np.asarray(solid_boundary_data.f_index_lt, dtype=np.int64).reshape(-1, d1),
+            device=context.device)
+        self.f_index_gt = torch.as_tensor(
+            np.asarray(solid_boundary_data.f_index_gt, dtype=np.int64).reshape(-1, d1),
+            device=context.device)
+        self.d_lt = context.convert_to_tensor(np.asarray(solid_boundary_data.d_lt).ravel())
+        self.d_gt = context.convert_to_tensor(np.asarray(solid_boundary_data.d_gt).ravel())
+        if len(self.d_lt) != len(self.f_index_lt) or len(self.d_gt) != len(self.f_index_gt):
+            raise ValueError("one wall distance per link")
+        self.calc_force = bool(calc_force)
+        self._force = None
+        if self.calc_force:
+            self._force = torch.zeros(3, dtype=torch.float64, device=context.device)
+
+    @property
+    def force_sum(self) -> torch.Tensor:
+        """momentum-exchange force of the last step's links, [D], context
+        dtype (lattice units); reading it applies a pending stream"""
+        if self._force is None:
+            raise AttributeError("force_sum needs calc_force=True")
+        self.flow._settle()
+        return self._force[:self.flow.stencil.d].to(self.context.dtype)
+
+    def link_rows(self):
+        """(link rows q, x, y[, z] as int64 [K, 1 + D], wall distances
+        float64 [K]) in the order lt, gt; the distances as the context
+        dtype holds them"""
+        rows = np.concatenate([self.f_index_lt.detach().cpu().numpy(),
+                               self.f_index_gt.detach().cpu().numpy()]).astype(np.int64)
+        dist = np.concatenate([self.d_lt.detach().cpu().double().numpy(),
+                               self.d_gt.detach().cpu().double().numpy()])
+        if np.any(dist < 0):
+            raise ValueError("wall distances must be >= 0")
+        return rows, dist
+
+    def __call__(self, flow):
+        raise RuntimeError("the interpolated bounce-back runs inside the step of an "
+                           "EbbSimulation")
+
+    def make_no_collision_mask(self, shape: List[int], context) -> torch.Tensor:
+        return torch.as_tensor(self.mask, device=context.device)
+
+    def make_no_streaming_mask(self, shape: List[int], context) -> torch.Tensor:
+        return torch.as_tensor(self.mask, device=context.device)
+
+    def native_available(self) -> bool:
+        return True
+
+    def native_generator(self, index: int) -> NativeBoundary:
         return NativeBoundary(_lib.SUB_NONE, index)

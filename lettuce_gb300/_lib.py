@@ -72,6 +72,11 @@ class StepDesc(ctypes.Structure):
                 ("reserved2", ctypes.c_int32),
                 ("mrt_tables", ctypes.c_void_p),
                 ("link_bits", ctypes.c_void_p),
+                ("link_base", ctypes.c_void_p),
+                ("link_pairs", ctypes.c_void_p),
+                ("link_d", ctypes.c_void_p),
+                ("link_val", ctypes.c_void_p),
+                ("n_links", ctypes.c_int64),
                 ("force_links", ctypes.c_void_p),
                 ("n_force_links", ctypes.c_int64),
                 ("force_out", ctypes.c_void_p)]

@@ -518,17 +518,20 @@ class EbbSimulation(Simulation):
     of ``HalfwayBounceBackBoundary`` runs inside the pull of the step kernel
     (per-cell link bits), so the steps run as one collide-only launch
     followed by pull launches, the last stream and bounce pending until the
-    field is read; ``_stream()`` called directly bounces as well. One
-    post-streaming boundary may compute its force."""
+    field is read; ``_stream()`` called directly bounces as well. The
+    ``LinearInterpolatedBounceBackBoundary`` adds a pass over its links
+    before each pulling launch that computes the interpolated values the
+    pull then reads. One post-streaming boundary may compute its force."""
 
     def __init__(self, flow, collision, reporter: List[Reporter],
                  use_graph: Optional[bool] = None):
-        from ._boundary import HalfwayBounceBackBoundary
+        from ._boundary import HalfwayBounceBackBoundary, LinearInterpolatedBounceBackBoundary
         psb = []
         if hasattr(flow.__class__, "post_streaming_boundaries"):
             psb = list(flow.post_streaming_boundaries or [])
         other = [b.__class__.__name__ for b in psb
-                 if not isinstance(b, HalfwayBounceBackBoundary)]
+                 if not isinstance(b, (HalfwayBounceBackBoundary,
+                                       LinearInterpolatedBounceBackBoundary))]
         if other:
             raise NotImplementedError(
                 f"no GB300 kernel for the post-streaming boundary {', '.join(other)}")
@@ -567,18 +570,59 @@ class EbbSimulation(Simulation):
         if not psb:
             return
         d = self._desc
-        bits = psb[0].link_bits()
-        for b in psb[1:]:
-            bits = bits | b.link_bits()
-        self._link_bits = bits.contiguous()
+        flow = self.flow
+        res = list(flow.resolution)
+        n_cells = int(np.prod(res))
+        opp = np.asarray(flow.stencil.opposite, dtype=np.int64)
+        parts = [b.link_rows() for b in psb]
+        rows = np.concatenate([r for r, _ in parts]).reshape(-1, len(res) + 1)
+        dist = np.concatenate([w for _, w in parts])
+        owner = np.concatenate([np.full(len(r), j) for j, (r, _) in enumerate(parts)])
+        coords = np.where(rows[:, 1:] < 0, rows[:, 1:] + np.array(res), rows[:, 1:])
+        cells = (np.ravel_multi_index(tuple(coords.T), tuple(res)) if len(rows)
+                 else np.zeros(0, dtype=np.int64))
+        q = rows[:, 0]
+        pop = opp[q]  # the population the link sets at its fluid cell
+        bits = np.zeros(n_cells, dtype=np.int64)
+        np.bitwise_or.at(bits, cells, np.left_shift(1, pop))
+        dev = self.context.device
+        self._link_bits = torch.as_tensor(bits.astype(np.uint32).view(np.int32).reshape(res),
+                                          device=dev).contiguous()
         self._flags |= (self._link_bits != 0).to(torch.uint8) * _lib.FLAG_LINKS
         d.link_bits = self._link_bits.data_ptr()
-        forcing = [b for b in psb if b.calc_force]
+        pos = np.full(len(rows), 0xFFFFFFFF, dtype=np.int64)
+        if np.any(dist >= 0):
+            # the value table: links sorted by cell, then by the population
+            # they set, so a cell's k-th link bit is its k-th entry
+            order = np.lexsort((pop, cells))
+            sc, sp = cells[order], pop[order]
+            if np.any((sc[1:] == sc[:-1]) & (sp[1:] == sp[:-1])):
+                raise ValueError("two links set the same population of one cell")
+            first = np.r_[True, sc[1:] != sc[:-1]]
+            base = np.zeros(n_cells, dtype=np.int64)
+            base[sc[first]] = np.nonzero(first)[0]
+            pairs = np.stack([q[order], sc], axis=1).astype(np.uint32)
+            vdt = self.context.storage_dtype  # the field's storage format
+            self._link_base = torch.as_tensor(base.astype(np.uint32).view(np.int32), device=dev)
+            self._link_pairs = torch.as_tensor(pairs.view(np.int32), device=dev).contiguous()
+            self._link_d = torch.as_tensor(dist[order], dtype=torch.float64, device=dev)
+            self._link_val = torch.zeros(len(order), dtype=vdt, device=dev)
+            d.link_base = self._link_base.data_ptr()
+            d.link_pairs = self._link_pairs.data_ptr()
+            d.link_d = self._link_d.data_ptr()
+            d.link_val = self._link_val.data_ptr()
+            d.n_links = len(order)
+            pos[order] = np.arange(len(order))
+        forcing = [j for j, b in enumerate(psb) if b.calc_force]
         if forcing:
-            self._force_links = forcing[0].force_links()
-            d.force_links = self._force_links.data_ptr() if len(self._force_links) else None
-            d.n_force_links = len(self._force_links)
-            d.force_out = forcing[0]._force.data_ptr()
+            sel = owner == forcing[0]
+            k = np.where(dist[sel] >= 0, pos[sel], 0xFFFFFFFF)
+            trip = np.stack([q[sel], cells[sel], k], axis=1).astype(np.uint32)
+            self._force_links = torch.as_tensor(np.ascontiguousarray(trip).view(np.int32),
+                                                device=dev)
+            d.force_links = self._force_links.data_ptr() if len(trip) else None
+            d.n_force_links = len(trip)
+            d.force_out = psb[forcing[0]]._force.data_ptr()
 
     def _choose_pull_post(self):
         if self._link_bits is not None:

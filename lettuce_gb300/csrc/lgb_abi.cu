@@ -407,21 +407,25 @@ cudaError_t launch_convert(int src_st, const void *src, int dst_st, void *dst, u
     return cudaErrorInvalidValue;
 }
 
-// Momentum exchange of halfway bounce-back links
-// (halfway_bounce_back_boundary.py:211-218): F = 2 sum_k f*_{q_k}(n_k) e_{q_k}
-// over the (q_k, n_k) pairs, read from the post-collision field. One block,
-// a fixed summation order: the result does not depend on scheduling.
-// Entries outside the field are skipped.
+// Momentum exchange of bounce-back links (halfway_bounce_back_boundary.py:
+// 211-218, linear_interpolated_bounce_back_boundary.py:104-126):
+// F = sum_k (g_k + b_k) e_{q_k}, g_k = f*_{q_k}(n_k) from the post-collision
+// field, b_k the bounced value (link_val[j_k], or g_k for a halfway link),
+// over the (q_k, n_k, j_k) triplets. One block, a fixed summation order:
+// the result does not depend on scheduling. Entries outside the field or
+// the value table are skipped.
 template <int SID, int ST>
 __global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t n_cells,
                                                          const uint32_t *links, int64_t n_links,
+                                                         const void *vals, int64_t n_vals,
                                                          double *out) {
     using S = lgb::Stencil<SID>;
     using Sto = lgb::Storage<ST>;
+    using R = typename Sto::R;
     __shared__ double part[3][256];
     double F[3] = {0.0, 0.0, 0.0};
     for (int64_t k = threadIdx.x; k < n_links; k += blockDim.x) {
-        const uint32_t q = links[2 * k], n = links[2 * k + 1];
+        const uint32_t q = links[3 * k], n = links[3 * k + 1], j = links[3 * k + 2];
         if (q >= (uint32_t)S::Q || (uint64_t)n >= n_cells) continue;
         double w = 0.0;
         int e[3] = {0, 0, 0};
@@ -435,8 +439,13 @@ __global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t
         }
         const double v = (double)Sto::load_plain(
             static_cast<const typename Sto::T *>(f) + (uint64_t)q * n_cells + n, w);
+        double b = v;
+        if (j != 0xffffffffu) {
+            if (!vals || (int64_t)j >= n_vals) continue;
+            b = (double)static_cast<const R *>(vals)[j];
+        }
 #pragma unroll
-        for (int d = 0; d < 3; ++d) F[d] += 2.0 * v * (double)e[d];
+        for (int d = 0; d < 3; ++d) F[d] += (v + b) * (double)e[d];
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) part[d][threadIdx.x] = F[d];
@@ -456,8 +465,69 @@ __global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t
 
 template <int SID, int ST>
 cudaError_t launch_link_force_ss(const void *f, uint64_t n_cells, const uint32_t *links,
-                                 int64_t n_links, double *out, cudaStream_t s) {
-    link_force_kernel<SID, ST><<<1, 256, 0, s>>>(f, n_cells, links, n_links, out);
+                                 int64_t n_links, const void *vals, int64_t n_vals, double *out,
+                                 cudaStream_t s) {
+    link_force_kernel<SID, ST><<<1, 256, 0, s>>>(f, n_cells, links, n_links, vals, n_vals, out);
+    return cudaGetLastError();
+}
+
+// The interpolated bounce-back values of one step
+// (linear_interpolated_bounce_back_boundary.py:55-96, in the EbbSimulation
+// order: the links read the post-collision field f* and, for d < 1/2, the
+// streamed value f_q(n) = f*_q(n - e_q)); one thread per link, computed in
+// the step's arithmetic type. Links outside the field are skipped.
+template <int SID, int ST>
+__global__ void __launch_bounds__(256) link_value_kernel(const void *f, uint32_t X, uint32_t Y,
+                                                         uint32_t Z, const uint32_t *pairs,
+                                                         const double *dist, int64_t n_links,
+                                                         void *vals) {
+    using S = lgb::Stencil<SID>;
+    using Sto = lgb::Storage<ST>;
+    using R = typename Sto::R;
+    const uint64_t N = (uint64_t)X * Y * Z;
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n_links) return;
+    const uint32_t q = pairs[2 * k], n = pairs[2 * k + 1];
+    if (q >= (uint32_t)S::Q || (uint64_t)n >= N) return;
+    double w = 0.0;
+    int qo = 0, ex = 0, ey = 0, ez = 0;
+#pragma unroll
+    for (int i = 0; i < S::Q; ++i) {
+        if ((uint32_t)i == q) {
+            w = S::w(i);
+            qo = S::opp(i);
+            ex = lgb::ix<S>(i);
+            ey = lgb::iy<S>(i);
+            ez = lgb::iz<S>(i);
+        }
+    }
+    const typename Sto::T *fp = static_cast<const typename Sto::T *>(f);
+    const R g = Sto::load_plain(fp + (uint64_t)q * N + n, w);
+    const R d = (R)dist[k];
+    R v;
+    if (d < R(0)) {
+        v = g;
+    } else if (d < R(0.5)) {
+        const uint32_t z = n % Z, row = n / Z, y = row % Y, x = row / Y;
+        const uint32_t xs = (x + X - (uint32_t)(ex + 1) + 1) % X;
+        const uint32_t ys = (y + Y - (uint32_t)(ey + 1) + 1) % Y;
+        const uint32_t zs = (z + Z - (uint32_t)(ez + 1) + 1) % Z;
+        const R streamed = Sto::load_plain(fp + (uint64_t)q * N + ((uint64_t)xs * Y + ys) * Z + zs, w);
+        v = R(2) * d * g + (R(1) - R(2) * d) * streamed;
+    } else {
+        const R go = Sto::load_plain(fp + (uint64_t)qo * N + n, w);
+        v = (R(1) / (R(2) * d)) * g + (R(1) - R(1) / (R(2) * d)) * go;
+    }
+    static_cast<R *>(vals)[k] = v;
+}
+
+template <int SID, int ST>
+cudaError_t launch_link_values_ss(const void *f, const Grid &g, const uint32_t *pairs,
+                                  const double *dist, int64_t n_links, void *vals,
+                                  cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n_links + 255) / 256);
+    link_value_kernel<SID, ST><<<blocks, 256, 0, s>>>(f, g.X, g.Y, g.Z, pairs, dist, n_links,
+                                                      vals);
     return cudaGetLastError();
 }
 
@@ -472,9 +542,18 @@ cudaError_t launch_link_force_ss(const void *f, uint64_t n_cells, const uint32_t
     }
 
 cudaError_t launch_link_force(int stencil, int storage, const void *f, uint64_t n_cells,
-                              const uint32_t *links, int64_t n_links, double *out,
-                              cudaStream_t s) {
-#define CALL(SID, ST) launch_link_force_ss<SID, ST>(f, n_cells, links, n_links, out, s)
+                              const uint32_t *links, int64_t n_links, const void *vals,
+                              int64_t n_vals, double *out, cudaStream_t s) {
+#define CALL(SID, ST) launch_link_force_ss<SID, ST>(f, n_cells, links, n_links, vals, n_vals, out, s)
+    LGB_SWITCH_SS(stencil, storage, CALL)
+#undef CALL
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_link_values(int stencil, int storage, const void *f, const Grid &g,
+                               const uint32_t *pairs, const double *dist, int64_t n_links,
+                               void *vals, cudaStream_t s) {
+#define CALL(SID, ST) launch_link_values_ss<SID, ST>(f, g, pairs, dist, n_links, vals, s)
     LGB_SWITCH_SS(stencil, storage, CALL)
 #undef CALL
     return cudaErrorInvalidValue;
@@ -655,13 +734,28 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
                         "(LGB_PULL, LGB_STREAM_ONLY) and ignored by LGB_LOCAL; pattern %d",
                         d->pattern);
         p.links = d->link_bits;
-    } else if (d->force_links || d->force_out) {
-        return fail("lgb_step: force_links / force_out without link_bits");
+        if (d->link_val) {
+            if (!d->link_base || !d->link_pairs || !d->link_d || d->n_links <= 0 ||
+                d->n_links > 0xffffffffLL)
+                return fail("lgb_step: interpolated links need link_base, link_pairs, link_d "
+                            "and 1..2^32-1 links (got %lld)", (long long)d->n_links);
+            p.link_base = d->link_base;
+            p.link_val = d->link_val;
+        }
+    } else if (d->force_links || d->force_out || d->link_val) {
+        return fail("lgb_step: force_links / force_out / link_val without link_bits");
     }
     if (d->force_out && (d->n_force_links < 0 || (d->n_force_links > 0 && !d->force_links)))
         return fail("lgb_step: %lld force links at %p", (long long)d->n_force_links,
                     (const void *)d->force_links);
     const bool streams = d->pattern == LGB_PULL || d->pattern == LGB_STREAM_ONLY;
+    if (p.link_val && streams) {
+        // the interpolated values come from f_in before the step reads them
+        cudaError_t el = launch_link_values(d->stencil, d->storage, d->f_in, g, d->link_pairs,
+                                            d->link_d, d->n_links, d->link_val,
+                                            static_cast<cudaStream_t>(stream));
+        if (el != cudaSuccess) return cuda_fail(el, "lgb_step: link value launch failed");
+    }
     // the kernel variant: BGK with a force is its own collision kind; the
     // patterns without a collision (stream only, AA unpack) run as such
     // whatever the descriptor's collision
@@ -680,7 +774,8 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (d->force_out && streams) {
         // f_in still holds the post-collision field the links bounced
         e = launch_link_force(d->stencil, d->storage, d->f_in, g.N, d->force_links,
-                              d->n_force_links, d->force_out, static_cast<cudaStream_t>(stream));
+                              d->n_force_links, d->link_val, d->n_links, d->force_out,
+                              static_cast<cudaStream_t>(stream));
         if (e != cudaSuccess) return cuda_fail(e, "lgb_step: link force launch failed");
     }
     return 0;

@@ -62,7 +62,9 @@ struct StepParams {
     CollideParams cp;
     const uint8_t *flags;
     const uint32_t *nsb;
-    const uint32_t *links;       // halfway bounce-back link bits, or null
+    const uint32_t *links;       // bounce-back link bits, or null
+    const uint32_t *link_base;   // interpolated links: first link of a cell
+    const void *link_val;        // interpolated links: bounced values (R), or null
     int32_t has_nsm;
     int32_t push_guard;  // the flags carry LGB_FLAG_PUSH_GUARD
     int32_t n_sub;
@@ -118,6 +120,7 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
     // opposite population; cells without either (nearly all) skip the
     // per-population test
     const bool keep_own = MASKED && LOAD == LOAD_PULL && (nsbits | lbits) != 0;
+    using T = typename Sto::T;
     auto load_all = [&](const bool check) {
 #pragma unroll
         for (int q = 0; q < S::Q; ++q) {
@@ -126,16 +129,23 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
             if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
                 src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
                 if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
-                if (check && q != 0) {
-                    // the bounce follows the stream (halfway_bounce_back_boundary.py:
-                    // 182-190 runs after ebb_simulation.py:76), so a link wins
-                    // over a no-streaming bit
-                    if ((lbits >> q) & 1u) { src = n; slot = S::opp(q); }
-                    else if ((nsbits >> q) & 1u) src = n;
-                }
             }
-            if constexpr (RAW) f[q] = Sto::load_h(fin + (size_t)slot * N + src);
-            else f[q] = Sto::load(fin + (size_t)slot * N + src, S::w(q));
+            const T *ptr = fin + (size_t)slot * N + src;
+            if (LOAD == LOAD_PULL && check && q != 0) {
+                // the bounce follows the stream (halfway_bounce_back_boundary.py:
+                // 182-190 runs after ebb_simulation.py:76), so a link wins
+                // over a no-streaming bit. A halfway link takes the cell's own
+                // post-collision opp(q); an interpolated one the value the
+                // link pass stored (same storage format)
+                if ((lbits >> q) & 1u)
+                    ptr = p.link_val ? static_cast<const T *>(p.link_val) + p.link_base[n] +
+                                           __popc(lbits & ((1u << q) - 1u))
+                                     : fin + (size_t)S::opp(q) * N + n;
+                else if ((nsbits >> q) & 1u)
+                    ptr = fin + (size_t)q * N + n;
+            }
+            if constexpr (RAW) f[q] = Sto::load_h(ptr);
+            else f[q] = Sto::load(ptr, S::w(q));
         }
     };
     if (keep_own) load_all(true);

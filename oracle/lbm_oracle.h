@@ -31,6 +31,8 @@
  *                   examples/advanced_projects/efficient_bounce_back_obstacle/
  *                   boundary/halfway_bounce_back_boundary.py:170-242 and
  *                   simulation/ebb_simulation.py:72-101
+ *   interpolated bounce-back (same project)
+ *                   boundary/linear_interpolated_bounce_back_boundary.py:55-153
  *
  * Parity of this restatement with lettuce itself is pinned by golden
  * vectors generated from lettuce (tests/golden/make_golden.py).
@@ -107,6 +109,14 @@ typedef struct {
     int64_t n_links;
     const int64_t *links;     /* [n_links][2]: q_k, flat cell index n_k */
     double *force_out;        /* [nsteps][3] or NULL */
+    /* linear interpolated bounce-back (Bouzidi): wall distance d_k of each
+     * link, < 0 for a halfway link (NULL: all halfway). With g = f*_{q_k}:
+     * d < 1/2: 2 d g + (1 - 2 d) f_{q_k}(n_k) (the streamed value),
+     * d >= 1/2: g / (2 d) + (1 - 1 / (2 d)) f*_{opp(q_k)}(n_k); all links
+     * read the field before any is bounced. The force of a step is
+     * sum_k (g_k + bounced_k) e_{q_k} (2 g_k e_{q_k} for a halfway link). */
+    const double *link_d;
+    const uint8_t *link_force; /* [n_links] 1 = counted in force_out; NULL = all */
 } orc_problem;
 
 int orc_stencil_dq(int stencil, int *d, int *q);

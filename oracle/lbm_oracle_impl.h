@@ -508,19 +508,41 @@ static int SFX(orc_run_impl)(const orc_problem *p, REAL *f, REAL *work, int nste
          * __call__ :170-190, calc_force_on_boundary :211-218, store_f_collided
          * :220-242) in the EbbSimulation order (simulation/ebb_simulation.py:72-76,
          * 93-101) */
-        REAL *fcol = (REAL *)malloc((size_t)p->n_links * sizeof(REAL));
+        /* the interpolated links follow linear_interpolated_bounce_back_boundary.py:
+         * store_f_collided :128-153, __call__ :55-96, calc_force_on_boundary :104-126 */
+        const int64_t K = p->n_links;
+        REAL *fcol = (REAL *)malloc((size_t)K * 3 * sizeof(REAL));
         if (!fcol) return -3;
+        REAL *fopp = fcol + K, *val = fcol + 2 * K;
         for (int s = 0; s < nsteps; ++s) {
             SFX(collide)(&g, p, cur, nthreads);
-            for (int64_t k = 0; k < p->n_links; ++k)
-                fcol[k] = cur[p->links[2 * k] * g.N + p->links[2 * k + 1]];
+            for (int64_t k = 0; k < K; ++k) {
+                const int q = (int)p->links[2 * k];
+                fcol[k] = cur[q * g.N + p->links[2 * k + 1]];
+                fopp[k] = cur[(int64_t)g.st->opp[q] * g.N + p->links[2 * k + 1]];
+            }
             SFX(stream)(&g, p, cur, nxt, nthreads);
             { REAL *t = cur; cur = nxt; nxt = t; }
-            double force[3] = {0.0, 0.0, 0.0};
-            for (int64_t k = 0; k < p->n_links; ++k) {
+            for (int64_t k = 0; k < K; ++k) {
                 const int q = (int)p->links[2 * k];
-                cur[(int64_t)g.st->opp[q] * g.N + p->links[2 * k + 1]] = fcol[k];
-                for (int d = 0; d < g.d; ++d) force[d] += 2.0 * (double)fcol[k] * g.st->e[q][d];
+                const REAL d = p->link_d ? (REAL)p->link_d[k] : (REAL)-1;
+                if (d < (REAL)0) {
+                    val[k] = fcol[k];
+                } else if (d < (REAL)0.5) {
+                    const REAL streamed = cur[q * g.N + p->links[2 * k + 1]];
+                    val[k] = (REAL)2 * d * fcol[k] + ((REAL)1 - (REAL)2 * d) * streamed;
+                } else {
+                    val[k] = ((REAL)1 / ((REAL)2 * d)) * fcol[k] +
+                             ((REAL)1 - (REAL)1 / ((REAL)2 * d)) * fopp[k];
+                }
+            }
+            double force[3] = {0.0, 0.0, 0.0};
+            for (int64_t k = 0; k < K; ++k) {
+                const int q = (int)p->links[2 * k];
+                cur[(int64_t)g.st->opp[q] * g.N + p->links[2 * k + 1]] = val[k];
+                if (p->link_force && !p->link_force[k]) continue;
+                for (int d = 0; d < g.d; ++d)
+                    force[d] += ((double)fcol[k] + (double)val[k]) * g.st->e[q][d];
             }
             if (p->force_out)
                 for (int d = 0; d < 3; ++d) p->force_out[3 * s + d] = force[d];

@@ -111,7 +111,9 @@ class _Problem(ctypes.Structure):
                 ("mrt_tables", ctypes.c_void_p),
                 ("n_links", ctypes.c_int64),
                 ("links", ctypes.c_void_p),
-                ("force_out", ctypes.c_void_p)]
+                ("force_out", ctypes.c_void_p),
+                ("link_d", ctypes.c_void_p),
+                ("link_force", ctypes.c_void_p)]
 
 
 def build():
@@ -253,11 +255,14 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
     "shan_chen" or None) with ``force_tau`` and ``accel`` (lattice units)
     applies to the BGK and Smagorinsky collisions. ``mrt`` = (equilibrium
     name, M, M^-1, relaxation times) for the "mrt" collision.
-    ``post_streaming``: halfway bounce-back boundaries, dicts with "solid"
-    (mask) and "f_index" (link rows q, x, y[, z]); with any, every step runs
-    collide, stream, bounce (the example EbbSimulation) whatever
-    ``strategy`` says, and ``forces`` (float64 [nsteps, 3], optional)
-    receives each step's momentum-exchange force over all links."""
+    ``post_streaming``: bounce-back boundaries of lettuce's example
+    project, dicts with "solid" (mask), "f_index" (link rows q, x, y[, z])
+    and, for the linear interpolated one, "d" (wall distance per row;
+    without it the links are halfway), "force" (default True: its links
+    count into ``forces``); with any, every step runs collide,
+    stream, bounce (the example EbbSimulation) whatever ``strategy`` says,
+    and ``forces`` (float64 [nsteps, 3], optional) receives each step's
+    momentum-exchange force over all links."""
     L = lib()
     f = np.ascontiguousarray(f)
     dt = f.dtype
@@ -331,9 +336,19 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
     p.sub = subs
     if post_streaming:
         links = np.concatenate([link_cells(b["f_index"], res) for b in post_streaming], axis=0)
-        keep.append(links)
+        dist = np.ascontiguousarray(np.concatenate(
+            [np.asarray(b["d"], dtype=np.float64).ravel() if "d" in b
+             else np.full(len(np.asarray(b["f_index"]).reshape(-1, len(res) + 1)), -1.0)
+             for b in post_streaming]))
+        counted = np.ascontiguousarray(np.concatenate(
+            [np.full(len(np.asarray(b["f_index"]).reshape(-1, len(res) + 1)),
+                     1 if b.get("force", True) else 0, dtype=np.uint8)
+             for b in post_streaming]))
+        keep += [links, dist, counted]
         p.n_links = len(links)
         p.links = links.ctypes.data
+        p.link_d = dist.ctypes.data
+        p.link_force = counted.ctypes.data
         if forces is not None:
             assert forces.dtype == np.float64 and forces.shape == (nsteps, 3)
             assert forces.flags["C_CONTIGUOUS"]

@@ -513,6 +513,79 @@ def case_hwbb(name, stencil, res, coll, steps, seed, solid, periodicity=None,
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
 
 
+def case_ibb(name, stencil, res, coll, steps, seed, solid, periodicity=None):
+    """lettuce's example linear interpolated bounce-back (Bouzidi et al.;
+    examples/advanced_projects/efficient_bounce_back_obstacle/boundary/
+    linear_interpolated_bounce_back_boundary.py) under the example's
+    EbbSimulation, with the momentum-exchange force after every step. The
+    links are the halfway bounce-back's neighbour search of the same solid;
+    each gets a wall distance drawn uniformly from [0.05, 0.95] by
+    numpy.random.default_rng(seed) after the populations, links with
+    d < 0.5 going to f_index_lt / d_lt and the others to f_index_gt / d_gt."""
+    import lettuce
+    root = os.path.dirname(os.path.dirname(os.path.abspath(lettuce.__file__)))
+    for sub in ("boundary", "simulation"):
+        d = os.path.join(root, EBB, sub)
+        if d not in sys.path:
+            sys.path.insert(0, d)
+    from halfway_bounce_back_boundary import HalfwayBounceBackBoundary
+    from linear_interpolated_bounce_back_boundary import LinearInterpolatedBounceBackBoundary
+    from solid_boundary_data import SolidBoundaryData
+    from ebb_simulation import EbbSimulation
+
+    class IbbFlow(GivenFlow):
+        psb = []
+
+        @property
+        def post_streaming_boundaries(self):
+            return self.psb
+
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.2 * rng.standard_normal([st.q] + res))
+    flow = IbbFlow(st, f0)
+    flow.context.d = st.d  # see case_hwbb
+    sbd = SolidBoundaryData()
+    sbd.solid_mask = solid
+    links = npf(HalfwayBounceBackBoundary(CTX, flow, sbd, periodicity=periodicity).f_index)
+    dist = rng.uniform(0.05, 0.95, size=len(links))
+    lt_ = dist < 0.5
+    sbd = SolidBoundaryData()
+    sbd.solid_mask = solid
+    sbd.f_index_lt, sbd.f_index_gt = links[lt_], links[~lt_]
+    sbd.d_lt, sbd.d_gt = dist[lt_], dist[~lt_]
+    ibb = LinearInterpolatedBounceBackBoundary(CTX, flow, sbd, calc_force=True)
+    flow.psb = [ibb]
+    tau = 0.8
+    sim = EbbSimulation(flow, collision_of(coll, tau), [])
+    out = {"f0": f0, "solid": solid, "tau": np.float64(tau), "steps": np.int64(steps),
+           "f_index_lt": sbd.f_index_lt.astype(np.int64), "f_index_gt": sbd.f_index_gt.astype(np.int64),
+           "d_lt": sbd.d_lt, "d_gt": sbd.d_gt,
+           "ncm": npf(sim.no_collision_mask).astype(np.uint8),
+           "nsm": npf(sim.no_streaming_mask).astype(np.uint8)}
+    forces = []
+    for _ in range(steps):
+        sim(1)
+        forces.append(npf(ibb.force_sum))
+    out["force"] = np.array(forces)
+    out["f"] = npf(flow.f)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res, "collision": coll,
+                              "periodicity": None if periodicity is None else list(periodicity),
+                              "inlet": False})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def ibb_cases():
+    g = np.meshgrid(np.arange(20), np.arange(12), indexing="ij")
+    solid = (g[0] - 8.0) ** 2 + (g[1] - 5.5) ** 2 < 3.1 ** 2
+    case_ibb("ibb_d2q9_bgk", D2Q9, [20, 12], "bgk", 6, 90, solid)
+    g = np.meshgrid(np.arange(10), np.arange(8), np.arange(6), indexing="ij")
+    solid = (g[0] - 4.5) ** 2 + (g[1] - 3.5) ** 2 + (g[2] - 2.5) ** 2 < 2.3 ** 2
+    case_ibb("ibb_d3q19_trt", D3Q19, [10, 8, 6], "trt", 4, 91, solid,
+             periodicity=(False, True, True))
+
+
 def hwbb_cases():
     # a disc inside a non-periodic 2-D box, and two blocks on the x = 0 and
     # x = 23 columns: the neighbour search wraps negative indices (Python
@@ -542,6 +615,9 @@ def main():
     torch.set_num_threads(os.cpu_count() or 1)
     if "--only-hwbb" in sys.argv:
         hwbb_cases()
+        return
+    if "--only-ibb" in sys.argv:
+        ibb_cases()
         return
     case_tgv("tgv2d_d2q9_bgk", D2Q9, 16, 1000, "bgk", 5)
     case_tgv("tgv2d_d2q9_trt", D2Q9, [16, 12], 300, "trt", 5)
@@ -579,6 +655,7 @@ def main():
     case_poiseuille("poiseuille_shanchen", "shan_chen", 300)
     case_dump()
     hwbb_cases()
+    ibb_cases()
     case_native_kats()
     case_observables()
     case_adjoint()

@@ -110,3 +110,17 @@ def hwbb_case(context, z, meta, f0=None):
                                       calc_force=True)
     flow.psb = [hw]
     return flow, hw
+
+
+def ibb_case(context, z, meta, f0=None):
+    """(flow, boundary) of an interpolated bounce-back golden case"""
+    stencil = getattr(lt, meta["stencil"])()
+    f0 = z["f0"] if f0 is None else f0
+    flow = HwbbFlow(context, stencil, f0)
+    sbd = lt.SolidBoundaryData()
+    sbd.solid_mask = z["solid"]
+    sbd.f_index_lt, sbd.f_index_gt = z["f_index_lt"], z["f_index_gt"]
+    sbd.d_lt, sbd.d_gt = z["d_lt"], z["d_gt"]
+    b = lt.LinearInterpolatedBounceBackBoundary(context, flow, sbd, calc_force=True)
+    flow.psb = [b]
+    return flow, b

@@ -116,3 +116,99 @@ def test_stream_half_alone_bounces(lgb):
         sim._stream()
     np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
     np.testing.assert_allclose(to_np(hw.force_sum), z["force"][-1], rtol=0, atol=1e-12)
+
+
+# -- the linear interpolated bounce-back of the same project ----------------
+
+IBB_CASES = golden_names("ibb_")
+
+
+def _ibb_sim(z, m, dtype=torch.float64, storage=None, use_graph=False, f0=None):
+    from lgb_helpers import ibb_case
+    ctx = lt.Context("cuda:0", dtype, storage=storage)
+    flow, b = ibb_case(ctx, z, m, f0=f0)
+    coll = lt.TRTCollision(float(z["tau"]), 1.0) if m["collision"] == "trt" else \
+        lt.BGKCollision(float(z["tau"]))
+    return lt.EbbSimulation(flow, coll, [], use_graph=use_graph), flow, b
+
+
+@pytest.mark.parametrize("name", IBB_CASES)
+def test_ibb_f64_matches_example_step_by_step(lgb, name):
+    z = golden(name)
+    m = meta(z)
+    sim, flow, b = _ibb_sim(z, m)
+    forces = []
+    for _ in range(int(z["steps"])):
+        sim(1)
+        forces.append(to_np(b.force_sum))
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(np.array(forces), z["force"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", IBB_CASES)
+def test_ibb_f64_graph_run_matches_example(lgb, name):
+    z = golden(name)
+    m = meta(z)
+    sim, flow, b = _ibb_sim(z, m, use_graph=True)
+    sim(int(z["steps"]))
+    np.testing.assert_allclose(to_np(b.force_sum), z["force"][-1], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("storage,tol", [(None, 2e-6), ("fp16_shifted", 2e-3)])
+def test_ibb_reduced_precision_against_oracle(lgb, oracle, storage, tol):
+    z = golden("ibb_d3q19_trt")
+    m = meta(z)
+    steps = 10
+    forces = np.zeros((steps, 3))
+    rows = np.concatenate([z["f_index_lt"], z["f_index_gt"]])
+    dist = np.concatenate([z["d_lt"], z["d_gt"]]).astype(np.float32)
+    ref = oracle.run(m["stencil"], z["f0"].astype(np.float32), steps, collision="trt",
+                     tau=float(z["tau"]), tau_minus=1.0,
+                     post_streaming=[dict(solid=z["solid"], f_index=rows, d=dist)],
+                     forces=forces)
+    sim, flow, b = _ibb_sim(z, m, torch.float32, storage, use_graph=True,
+                            f0=z["f0"].astype(np.float32))
+    sim(steps)
+    assert rel_max(to_np(flow.f), ref) < tol
+    assert rel_max(to_np(b.force_sum), forces[-1]) < 50 * tol
+
+
+def test_halfway_and_interpolated_together(lgb, oracle):
+    """two post-streaming boundaries on separate solids, a halfway one and
+    an interpolated one that computes the force, against the oracle"""
+    zh = golden("hwbb_d2q9_bgk")
+    st = lt.D2Q9()
+    g = np.meshgrid(np.arange(24), np.arange(14), indexing="ij")
+    solid_i = (g[0] - 18.0) ** 2 + (g[1] - 6.5) ** 2 < 2.2 ** 2
+    assert not np.any(solid_i & zh["solid"])
+    both = zh["solid"] | solid_i
+    rows_i = lt.hwbb_links(st.e, st.opposite, solid_i, both)
+    d_i = np.random.default_rng(3).uniform(0.05, 0.95, len(rows_i))
+    small = d_i < 0.5
+    ctx = lt.Context("cuda:0", torch.float64)
+    from lgb_helpers import HwbbFlow
+    flow = HwbbFlow(ctx, st, zh["f0"])
+    sh = lt.SolidBoundaryData()
+    sh.solid_mask = zh["solid"]
+    hw = lt.HalfwayBounceBackBoundary(ctx, flow, sh, global_solid_mask=both)
+    si = lt.SolidBoundaryData()
+    si.solid_mask = solid_i
+    si.f_index_lt, si.f_index_gt = rows_i[small], rows_i[~small]
+    si.d_lt, si.d_gt = d_i[small], d_i[~small]
+    ib = lt.LinearInterpolatedBounceBackBoundary(ctx, flow, si, calc_force=True)
+    flow.psb = [hw, ib]
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.8), [], use_graph=True)
+    steps = 7
+    sim(steps)
+    forces = np.zeros((steps, 3))
+    ref = oracle.run("D2Q9", zh["f0"], steps, collision="bgk", tau=0.8,
+                     post_streaming=[dict(solid=zh["solid"], f_index=hw.f_index.cpu().numpy(),
+                                          force=False),
+                                     dict(solid=solid_i,
+                                          f_index=np.concatenate([rows_i[small], rows_i[~small]]),
+                                          d=np.concatenate([d_i[small], d_i[~small]]))],
+                     forces=forces)
+    np.testing.assert_allclose(to_np(flow.f), ref, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(to_np(ib.force_sum), forces[-1, :2], rtol=0, atol=1e-12)
+    assert sim.status == 0

@@ -1,6 +1,6 @@
-"""Halfway bounce-back of lettuce's example project (the post-streaming
-boundary of examples/advanced_projects/efficient_bounce_back_obstacle), on
-CPU: the oracle against the golden vectors the example itself produced
+"""Halfway and linear interpolated bounce-back of lettuce's example project
+(the post-streaming boundaries of
+examples/advanced_projects/efficient_bounce_back_obstacle), on CPU: the oracle against the golden vectors the example itself produced
 (populations after every step's collide, stream, bounce, and the
 momentum-exchange force of each step), the product's neighbour search
 against the example's link lists, and the masks, link bits and force links
@@ -11,9 +11,10 @@ import torch
 
 import lettuce_gb300 as lt
 from conftest import golden, golden_names, meta
-from lgb_helpers import hwbb_case
+from lgb_helpers import hwbb_case, ibb_case
 
 CASES = golden_names("hwbb_")
+IBB_CASES = golden_names("ibb_")
 
 
 def _post(z, m):
@@ -96,13 +97,15 @@ def test_ebb_masks_and_links_on_cpu(name):
     assert np.array_equal((flags & lt._lib.FLAG_LINKS) != 0, want != 0)
     assert not np.any(z["solid"] & (want != 0))          # links sit on fluid cells
     assert int(sim._desc.link_bits) == sim._link_bits.data_ptr()
-    pairs = sim._force_links.numpy().view(np.uint32)
-    assert pairs.shape == (len(z["f_index"]), 2)
+    trip = sim._force_links.numpy().view(np.uint32)
+    assert trip.shape == (len(z["f_index"]), 3)
     flat = np.ravel_multi_index(tuple(np.where(z["f_index"][:, 1:] < 0,
                                                z["f_index"][:, 1:] + res,
                                                z["f_index"][:, 1:]).T), tuple(res))
-    assert np.array_equal(pairs[:, 0], z["f_index"][:, 0]) and np.array_equal(pairs[:, 1], flat)
-    assert sim._pull_post and sim._desc.n_force_links == len(pairs)
+    assert np.array_equal(trip[:, 0], z["f_index"][:, 0]) and np.array_equal(trip[:, 1], flat)
+    assert np.all(trip[:, 2] == 0xFFFFFFFF)       # halfway links: no value table
+    assert sim._pull_post and sim._desc.n_force_links == len(trip)
+    assert not sim._desc.link_val
 
 
 def test_ebb_rejections_on_cpu():
@@ -125,3 +128,59 @@ def test_ebb_rejections_on_cpu():
         lt.SlabSimulation(sim, 2)
     with pytest.raises(RuntimeError, match="CUDA"):
         sim(1)
+
+
+def _ibb_rows(z):
+    return (np.concatenate([z["f_index_lt"], z["f_index_gt"]]),
+            np.concatenate([z["d_lt"], z["d_gt"]]))
+
+
+def test_ibb_cases_present():
+    assert len(IBB_CASES) == 2
+
+
+@pytest.mark.parametrize("name", IBB_CASES)
+def test_oracle_matches_example_interpolated(oracle, name):
+    z = golden(name)
+    m = meta(z)
+    steps = int(z["steps"])
+    forces = np.zeros((steps, 3))
+    rows, dist = _ibb_rows(z)
+    out = oracle.run(m["stencil"], z["f0"], steps, collision=m["collision"],
+                     tau=float(z["tau"]), tau_minus=1.0,
+                     post_streaming=[dict(solid=z["solid"], f_index=rows, d=dist)],
+                     forces=forces)
+    np.testing.assert_allclose(out, z["f"], rtol=0, atol=1e-14)
+    d = len(m["res"])
+    np.testing.assert_allclose(forces[:, :d], z["force"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", IBB_CASES)
+def test_ibb_value_table_on_cpu(name):
+    """the sorted link table: a cell's k-th link bit (in population order)
+    is entry base[cell] + k, whose pair names the link's population into
+    the solid and the cell; the force triplets point at their links"""
+    z = golden(name)
+    m = meta(z)
+    flow, b = ibb_case(lt.Context("cpu", torch.float64), z, m)
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.8), [])
+    assert np.array_equal(sim.no_collision_mask.numpy(), z["ncm"])
+    assert np.array_equal(sim.no_streaming_mask.numpy(), z["nsm"])
+    st = flow.stencil
+    bits = sim._link_bits.numpy().reshape(-1).view(np.uint32)
+    base = sim._link_base.numpy().view(np.uint32)
+    pairs = sim._link_pairs.numpy().view(np.uint32)
+    dist = sim._link_d.numpy()
+    rows, d0 = _ibb_rows(z)
+    assert len(pairs) == len(rows) == sim._desc.n_links
+    for j, (q, cell) in enumerate(pairs):
+        pop = st.opposite[q]
+        below = bin(int(bits[cell]) & ((1 << pop) - 1)).count("1")
+        assert (bits[cell] >> pop) & 1 and base[cell] + below == j
+    res = np.array(m["res"])
+    flat = np.ravel_multi_index(tuple(rows[:, 1:].T), tuple(res))
+    got = {(int(q), int(c)): float(w) for (q, c), w in zip(pairs, dist)}
+    assert got == {(int(q), int(c)): float(w) for q, c, w in zip(rows[:, 0], flat, d0)}
+    trip = sim._force_links.numpy().view(np.uint32)
+    assert np.array_equal(pairs[trip[:, 2]], trip[:, :2])
+    assert sim._link_val.dtype == flow.context.storage_dtype and len(sim._link_val) == len(rows)
