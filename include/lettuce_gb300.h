@@ -156,8 +156,9 @@ typedef struct {
      * distance d (< 0: a halfway link, f*_q(n)); g = f*_q(n):
      *   d < 1/2:  2 d g + (1 - 2 d) f*_q(n - e_q)
      *   d >= 1/2: g / (2 d) + (1 - 1 / (2 d)) f*_{opp(q)}(n).
-     * link_val is scratch in the compute type (double for LGB_F64, float
-     * otherwise). NULL link_val: every link is a halfway link. */
+     * link_val is scratch of n_links elements in the field's storage format
+     * (the interpolated value is stored like any population). NULL
+     * link_val: every link is a halfway link. */
     const uint32_t *link_base;   /* [N] */
     const uint32_t *link_pairs;  /* [n_links][2] */
     const double *link_d;        /* [n_links] */

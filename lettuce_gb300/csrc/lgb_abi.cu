@@ -421,7 +421,6 @@ __global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t
                                                          double *out) {
     using S = lgb::Stencil<SID>;
     using Sto = lgb::Storage<ST>;
-    using R = typename Sto::R;
     __shared__ double part[3][256];
     double F[3] = {0.0, 0.0, 0.0};
     for (int64_t k = threadIdx.x; k < n_links; k += blockDim.x) {
@@ -442,7 +441,7 @@ __global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t
         double b = v;
         if (j != 0xffffffffu) {
             if (!vals || (int64_t)j >= n_vals) continue;
-            b = (double)static_cast<const R *>(vals)[j];
+            b = (double)Sto::load_plain(static_cast<const typename Sto::T *>(vals) + j, w);
         }
 #pragma unroll
         for (int d = 0; d < 3; ++d) F[d] += (v + b) * (double)e[d];
@@ -475,7 +474,9 @@ cudaError_t launch_link_force_ss(const void *f, uint64_t n_cells, const uint32_t
 // (linear_interpolated_bounce_back_boundary.py:55-96, in the EbbSimulation
 // order: the links read the post-collision field f* and, for d < 1/2, the
 // streamed value f_q(n) = f*_q(n - e_q)); one thread per link, computed in
-// the step's arithmetic type. Links outside the field are skipped.
+// the step's arithmetic type and stored in the field's storage format (the
+// table holds one storage element per link). Links outside the field are
+// skipped.
 template <int SID, int ST>
 __global__ void __launch_bounds__(256) link_value_kernel(const void *f, uint32_t X, uint32_t Y,
                                                          uint32_t Z, const uint32_t *pairs,
@@ -518,7 +519,7 @@ __global__ void __launch_bounds__(256) link_value_kernel(const void *f, uint32_t
         const R go = Sto::load_plain(fp + (uint64_t)qo * N + n, w);
         v = (R(1) / (R(2) * d)) * g + (R(1) - R(1) / (R(2) * d)) * go;
     }
-    static_cast<R *>(vals)[k] = v;
+    Sto::store(static_cast<typename Sto::T *>(vals) + k, v, w);
 }
 
 template <int SID, int ST>
