@@ -110,7 +110,7 @@ template <> struct PatternTraits<LGB_AA_ODD> { static constexpr int load = LOAD_
 template <> struct PatternTraits<LGB_AA_UNPACK> { static constexpr int load = LOAD_AA_ODD; };
 
 // populations of the cell `c` (index n) as the collide phase sees them
-template <class S, class Sto, int LOAD, bool MASKED, bool RAW = false>
+template <class S, class Sto, int LOAD, bool MASKED, bool RAW = false, bool LINKS = false>
 __device__ __forceinline__ void load_cell(const StepParams &p, const typename Sto::T *__restrict__ fin,
                                           const Nbr &c, uint32_t n, uint32_t nsbits,
                                           typename Sto::R (&f)[S::Q], uint32_t lbits = 0) {
@@ -119,7 +119,7 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
     // populations, and a halfway bounce-back link takes the cell's own
     // opposite population; cells without either (nearly all) skip the
     // per-population test
-    const bool keep_own = MASKED && LOAD == LOAD_PULL && (nsbits | lbits) != 0;
+    const bool keep_own = MASKED && LOAD == LOAD_PULL && (nsbits | (LINKS ? lbits : 0u)) != 0;
     using T = typename Sto::T;
     auto load_all = [&](const bool check) {
 #pragma unroll
@@ -137,7 +137,7 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
                 // over a no-streaming bit. A halfway link takes the cell's own
                 // post-collision opp(q); an interpolated one the value the
                 // link pass stored (same storage format)
-                if ((lbits >> q) & 1u)
+                if (LINKS && ((lbits >> q) & 1u))
                     ptr = p.link_val ? static_cast<const T *>(p.link_val) + p.link_base[n] +
                                            __popc(lbits & ((1u << q) - 1u))
                                      : fin + (size_t)S::opp(q) * N + n;
@@ -234,7 +234,7 @@ __device__ __forceinline__ uint32_t coord_along(const Nbr &c, int axis) {
 // (equilibrium_outlet_p.py:61-71). The neighbour one cell inside is rebuilt
 // as the collide phase sees it at substep abb_k (its populations after the
 // substeps before abb_k).
-template <class S, int COLL, int LOAD, bool MASKED, class Sto, class TT>
+template <class S, int COLL, int LOAD, bool MASKED, bool LINKS, class Sto, class TT>
 __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename Sto::T *__restrict__ fin,
                                              const Nbr &c, typename Sto::R (&f)[S::Q], const TT &tab) {
     using R = typename Sto::R;
@@ -245,9 +245,10 @@ __device__ __forceinline__ void apply_outlet(const StepParams &p, const typename
     const uint32_t nn = (xn * p.Y + yn) * p.Z + zn;
     const uint8_t fl = p.flags[nn];
     const uint32_t nsb = ((fl & LGB_FLAG_NO_STREAM) && p.nsb) ? p.nsb[nn] : 0u;
-    const uint32_t lb = (LOAD == LOAD_PULL && (fl & LGB_FLAG_LINKS) && p.links) ? p.links[nn] : 0u;
+    const uint32_t lb =
+        (LINKS && LOAD == LOAD_PULL && (fl & LGB_FLAG_LINKS) && p.links) ? p.links[nn] : 0u;
     R g[S::Q];
-    load_cell<S, Sto, LOAD, MASKED>(p, fin, cn, nn, nsb, g, lb);
+    load_cell<S, Sto, LOAD, MASKED, false, LINKS>(p, fin, cn, nn, nsb, g, lb);
     const int idx = fl & LGB_FLAG_INDEX_MASK;
     if (idx < p.abb_k) apply_local_substep<S, COLL>(p, select_sub(p, idx), cn, g, tab);
     R rho, u[3], rn, un[3];
@@ -284,7 +285,9 @@ __device__ __forceinline__ void store_value(typename Sto::T *ptr, typename Sto::
 
 // MASK: 0 = no boundaries; 1 = boundaries, every cell except those of the
 // anti-bounce-back outlet plane (when there is one); 2 = the outlet plane
-// only (one thread per plane cell). Splitting the outlet off keeps its extra
+// only (one thread per plane cell); 3 and 4 = 1 and 2 with bounce-back links
+// (only these variants carry the link code, so the others keep their
+// register budget). Splitting the outlet off keeps its extra
 // neighbour reconstruction out of the register budget of the bulk launch.
 // The step of one cell; the kernels below wrap it with their launch bounds.
 template <int SID, int ST, int COLL, int PAT, int MASK, class TT>
@@ -294,6 +297,9 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     using R = typename Sto::R;
     using T = typename Sto::T;
     constexpr bool MASKED = MASK != 0;
+    constexpr bool PLANE = MASK == 2 || MASK == 4;
+    constexpr bool BULK = MASK == 1 || MASK == 3;
+    constexpr bool LINKS = MASK >= 3;
     constexpr bool SUBSTEPS = PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK;
     constexpr int LOAD = PatternTraits<PAT>::load;
     // 16-bit formats without boundaries collide in shifted space, with the
@@ -302,7 +308,7 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     const T *__restrict__ fin = static_cast<const T *>(p.f_in);
     T *fout = static_cast<T *>(p.f_out);
     uint32_t n, x, y, z;
-    if constexpr (MASK == 2) {
+    if constexpr (PLANE) {
         // plane cell i -> (x, y, z) with the normal coordinate fixed
         const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
         const uint32_t a = p.abb_axis == 0 ? p.Y : p.X;  // first free axis extent
@@ -323,7 +329,7 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     }
     Nbr c;
     c.set(x, y, z, p);
-    if constexpr (MASK == 1 && SUBSTEPS) {
+    if constexpr (BULK && SUBSTEPS) {
         // the outlet plane has its own launch
         if (p.abb_k >= 0 && coord_along(c, p.abb_axis) == p.abb_plane) return;
     }
@@ -333,16 +339,16 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     if (MASKED) {
         fl = p.flags[n];
         if ((fl & LGB_FLAG_NO_STREAM) && p.nsb) nsbits = p.nsb[n];
-        if (LOAD == LOAD_PULL && (fl & LGB_FLAG_LINKS) && p.links) lbits = p.links[n];
+        if (LINKS && LOAD == LOAD_PULL && (fl & LGB_FLAG_LINKS) && p.links) lbits = p.links[n];
     }
     R f[S::Q];
-    load_cell<S, Sto, LOAD, MASKED, HSPACE>(p, fin, c, n, nsbits, f, lbits);
+    load_cell<S, Sto, LOAD, MASKED, HSPACE, LINKS>(p, fin, c, n, nsbits, f, lbits);
 
     if constexpr (HSPACE) {
         if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK)
             collide_shifted<S, Lane1, COLL>(f, p.cp);
     } else if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK) {
-        if constexpr (MASK == 1) {
+        if constexpr (BULK) {
             // a cell off the outlet plane runs the substep its index names;
             // the collision (most cells) without copying out a substep record
             const int idx = fl & LGB_FLAG_INDEX_MASK;
@@ -352,7 +358,7 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
             } else {
                 apply_local_substep<S, COLL, false>(p, select_sub(p, idx), c, f, tab);
             }
-        } else if constexpr (MASK == 2) {
+        } else if constexpr (PLANE) {
             // an outlet-plane cell runs the substep its index names and the
             // outlet substep, in sequence order
             const int idx = fl & LGB_FLAG_INDEX_MASK;
@@ -363,7 +369,7 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
                 if (phase != outlet_phase && idx != p.abb_k)
                     apply_local_substep<S, COLL>(p, select_sub(p, idx), c, f, tab);
                 if (phase == outlet_phase && outlet)
-                    apply_outlet<S, COLL, LOAD, MASKED, Sto>(p, fin, c, f, tab);
+                    apply_outlet<S, COLL, LOAD, MASKED, LINKS, Sto>(p, fin, c, f, tab);
             }
         } else {
             R r;
@@ -459,15 +465,16 @@ template <int SID, int ST, int COLL, int PAT, int MASK>
 cudaError_t launch_step(const StepParams &p, cudaStream_t stream) {
     // the outlet plane has few cells (128 x 128 for the obstacle): smaller
     // blocks spread them over more SMs
-    const unsigned threads = MASK == 2 ? 64 : 256;
+    constexpr bool PLANE = MASK == 2 || MASK == 4;
+    const unsigned threads = PLANE ? 64 : 256;
     uint64_t count = p.N;
-    if (MASK == 2) {
+    if (PLANE) {
         const uint32_t ax = p.abb_axis == 0 ? p.X : (p.abb_axis == 1 ? p.Y : p.Z);
         count = p.N / ax;
     }
     const unsigned blocks = (unsigned)((count + threads - 1) / threads);
     const StepTables<SID, ST, COLL> tab = make_tables<SID, ST, COLL>(p);
-    if constexpr (COLL == LGB_KBC && SID == LGB_D3Q27 && MASK != 2)
+    if constexpr (COLL == LGB_KBC && SID == LGB_D3Q27 && !PLANE)
         step_kernel_bounded<SID, ST, COLL, PAT, MASK><<<blocks, threads, 0, stream>>>(p, tab);
     else
         step_kernel<SID, ST, COLL, PAT, MASK><<<blocks, threads, 0, stream>>>(p, tab);
@@ -485,31 +492,41 @@ template <int SID> constexpr bool has_kbc() { return SID == LGB_D2Q9 || SID == L
 cudaStream_t fork_aux(cudaStream_t s);
 cudaError_t join_aux(cudaStream_t s, cudaStream_t aux);
 
+template <int SID, int ST, int COLL, int PAT, int BULK, int PLANE>
+cudaError_t launch_masked(const StepParams &p, cudaStream_t s) {
+    constexpr bool SUBSTEPS = PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK;
+    constexpr bool OUTLET = SUBSTEPS && PAT != LGB_AA_EVEN && PAT != LGB_AA_ODD;
+    if constexpr (OUTLET) {
+        if (p.abb_k >= 0) {
+            // the outlet plane and the bulk write disjoint populations
+            // (every destination slot has one writer) and only read the
+            // input field: the short plane launch runs beside the bulk
+            cudaStream_t aux = fork_aux(s);
+            if (aux) {
+                const cudaError_t e2 = launch_step<SID, ST, COLL, PAT, PLANE>(p, aux);
+                const cudaError_t e1 = launch_step<SID, ST, COLL, PAT, BULK>(p, s);
+                const cudaError_t e3 = join_aux(s, aux);
+                return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+            }
+            const cudaError_t e = launch_step<SID, ST, COLL, PAT, BULK>(p, s);
+            if (e != cudaSuccess) return e;
+            return launch_step<SID, ST, COLL, PAT, PLANE>(p, s);
+        }
+    }
+    return launch_step<SID, ST, COLL, PAT, BULK>(p, s);
+}
+
 template <int SID, int ST, int COLL, int PAT, bool MASKED>
 cudaError_t launch_step_set(const StepParams &p, cudaStream_t s) {
     if constexpr (!MASKED) {
         return launch_step<SID, ST, COLL, PAT, 0>(p, s);
     } else {
-        constexpr bool SUBSTEPS = PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK;
-        constexpr bool OUTLET = SUBSTEPS && PAT != LGB_AA_EVEN && PAT != LGB_AA_ODD;
-        if constexpr (OUTLET) {
-            if (p.abb_k >= 0) {
-                // the outlet plane and the bulk write disjoint populations
-                // (every destination slot has one writer) and only read the
-                // input field: the short plane launch runs beside the bulk
-                cudaStream_t aux = fork_aux(s);
-                if (aux) {
-                    const cudaError_t e2 = launch_step<SID, ST, COLL, PAT, 2>(p, aux);
-                    const cudaError_t e1 = launch_step<SID, ST, COLL, PAT, 1>(p, s);
-                    const cudaError_t e3 = join_aux(s, aux);
-                    return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
-                }
-                const cudaError_t e = launch_step<SID, ST, COLL, PAT, 1>(p, s);
-                if (e != cudaSuccess) return e;
-                return launch_step<SID, ST, COLL, PAT, 2>(p, s);
-            }
+        // bounce-back links act in the pulling patterns only (LGB_LOCAL
+        // ignores them)
+        if constexpr (PAT == LGB_PULL || PAT == LGB_STREAM_ONLY) {
+            if (p.links) return launch_masked<SID, ST, COLL, PAT, 3, 4>(p, s);
         }
-        return launch_step<SID, ST, COLL, PAT, 1>(p, s);
+        return launch_masked<SID, ST, COLL, PAT, 1, 2>(p, s);
     }
 }
 
