@@ -29,6 +29,10 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                      "-I", INCLUDE, "-I", CSRC]
 
 STEP_STENCILS = ["d1q3", "d2q9", "d3q15", "d3q19", "d3q27"]
+# stencils whose units are split into grids without boundaries and, with
+# boundaries, the pulling and the other patterns (their instantiations take
+# the longest to compile)
+SPLIT_STENCILS = ("d3q19", "d3q27")
 N_STORAGES = 4
 
 
@@ -46,12 +50,15 @@ def _units():
     """(object name, source, extra flags) for every translation unit"""
     units = []
     for st in STEP_STENCILS:
+        parts = [("_p0", ["-DLGB_MASK_PART=0"]), ("_p1", ["-DLGB_MASK_PART=1"]),
+                 ("_p3", ["-DLGB_MASK_PART=3"])] if st in SPLIT_STENCILS else [("", [])]
         for s in range(N_STORAGES):
-            units.append((f"step_{st}_s{s}.o", f"lgb_step_{st}.cu",
-                          [f"-DLGB_STORAGE_ID={s}"]))
-            # forced BGK, regularized and Smagorinsky: their own objects
-            units.append((f"stepx_{st}_s{s}.o", f"lgb_step_{st}.cu",
-                          [f"-DLGB_STORAGE_ID={s}", "-DLGB_EXT_COLLISIONS=1"]))
+            for tag, part in parts:
+                units.append((f"step_{st}_s{s}{tag}.o", f"lgb_step_{st}.cu",
+                              [f"-DLGB_STORAGE_ID={s}"] + part))
+                # forced BGK, regularized, Smagorinsky and MRT: their own objects
+                units.append((f"stepx_{st}_s{s}{tag}.o", f"lgb_step_{st}.cu",
+                              [f"-DLGB_STORAGE_ID={s}", "-DLGB_EXT_COLLISIONS=1"] + part))
     for src in sorted(os.listdir(CSRC)):
         if src.endswith(".cu") and not src.startswith("lgb_step_"):
             units.append((src[:-3] + ".o", src, []))
@@ -106,6 +113,9 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             print(f"[lettuce_gb300] built {obj}", file=sys.stderr)
         return obj, key
 
+    # longest first, so the last units to finish are short ones
+    cost = {"d3q27": 0, "d3q19": 1, "batched": 2, "abi": 3, "d3q15": 4}
+    todo.sort(key=lambda it: min([v for k, v in cost.items() if k in it[0]] + [9]))
     jobs = jobs or max(1, os.cpu_count() or 1)
     if todo:
         with cf.ThreadPoolExecutor(max_workers=jobs) as ex:

@@ -141,13 +141,17 @@ namespace {
 
 cudaError_t dispatch_step(int stencil, int storage, int coll, int pat, bool masked,
                           const lgb::StepParams &p, cudaStream_t s) {
-#define LGB_STORAGE_SWITCH(name)                                            \
-    switch (storage) {                                                      \
-    case 0: return lgb::name##_s0(coll, pat, masked, p, s);                 \
-    case 1: return lgb::name##_s1(coll, pat, masked, p, s);                 \
-    case 2: return lgb::name##_s2(coll, pat, masked, p, s);                 \
-    case 3: return lgb::name##_s3(coll, pat, masked, p, s);                 \
-    }                                                                       \
+#define LGB_PART_CALL(name, st)                                                             \
+    (!masked ? lgb::name##_plain_##st(coll, pat, p, s)                                      \
+             : lgb::pulling_pattern(pat) ? lgb::name##_masked_pull_##st(coll, pat, p, s)   \
+                                         : lgb::name##_masked_rest_##st(coll, pat, p, s))
+#define LGB_STORAGE_SWITCH(name)                                                            \
+    switch (storage) {                                                                      \
+    case 0: return LGB_PART_CALL(name, s0);                                                 \
+    case 1: return LGB_PART_CALL(name, s1);                                                 \
+    case 2: return LGB_PART_CALL(name, s2);                                                 \
+    case 3: return LGB_PART_CALL(name, s3);                                                 \
+    }                                                                                       \
     return cudaErrorInvalidValue;
     const bool ext = coll == lgb::LGB_BGK_FORCED || coll == LGB_REGULARIZED ||
                      coll == LGB_SMAGORINSKY || coll == LGB_MRT;
@@ -169,6 +173,7 @@ cudaError_t dispatch_step(int stencil, int storage, int coll, int pat, bool mask
     case LGB_D3Q27: LGB_STORAGE_SWITCH(step_d3q27)
     }
 #undef LGB_STORAGE_SWITCH
+#undef LGB_PART_CALL
     return cudaErrorInvalidValue;
 }
 

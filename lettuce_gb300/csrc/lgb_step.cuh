@@ -559,31 +559,59 @@ cudaError_t dispatch_collision(int coll, const StepParams &p, cudaStream_t s) {
     }
 }
 
-template <int SID, int ST, bool MASKED, bool EXT>
+// pattern sets of one instantiation unit: the pulling patterns (the ones
+// that carry bounce-back links) and the others
+enum PatternSet { PATTERNS_ALL = 0, PATTERNS_PULLING = 1, PATTERNS_OTHER = 2 };
+__host__ __device__ constexpr bool pulling_pattern(int pat) {
+    return pat == LGB_PULL || pat == LGB_STREAM_ONLY;
+}
+
+template <int SID, int ST, bool MASKED, bool EXT, int SET = PATTERNS_ALL>
 cudaError_t dispatch_pattern(int coll, int pat, const StepParams &p, cudaStream_t s) {
+    constexpr bool PULLING = SET != PATTERNS_OTHER;
+    constexpr bool OTHER = SET != PATTERNS_PULLING;
     switch (pat) {
-    case LGB_PULL: return dispatch_collision<SID, ST, LGB_PULL, MASKED, EXT>(coll, p, s);
-    case LGB_PUSH: return dispatch_collision<SID, ST, LGB_PUSH, MASKED, EXT>(coll, p, s);
-    case LGB_LOCAL: return dispatch_collision<SID, ST, LGB_LOCAL, MASKED, EXT>(coll, p, s);
-    case LGB_AA_EVEN: return dispatch_collision<SID, ST, LGB_AA_EVEN, MASKED, EXT>(coll, p, s);
-    case LGB_AA_ODD: return dispatch_collision<SID, ST, LGB_AA_ODD, MASKED, EXT>(coll, p, s);
+    case LGB_PULL:
+        if constexpr (PULLING) return dispatch_collision<SID, ST, LGB_PULL, MASKED, EXT>(coll, p, s);
+        break;
     case LGB_STREAM_ONLY:
-        return dispatch_collision<SID, ST, LGB_STREAM_ONLY, MASKED, EXT>(coll, p, s);
+        if constexpr (PULLING)
+            return dispatch_collision<SID, ST, LGB_STREAM_ONLY, MASKED, EXT>(coll, p, s);
+        break;
+    case LGB_PUSH:
+        if constexpr (OTHER) return dispatch_collision<SID, ST, LGB_PUSH, MASKED, EXT>(coll, p, s);
+        break;
+    case LGB_LOCAL:
+        if constexpr (OTHER) return dispatch_collision<SID, ST, LGB_LOCAL, MASKED, EXT>(coll, p, s);
+        break;
+    case LGB_AA_EVEN:
+        if constexpr (OTHER) return dispatch_collision<SID, ST, LGB_AA_EVEN, MASKED, EXT>(coll, p, s);
+        break;
+    case LGB_AA_ODD:
+        if constexpr (OTHER) return dispatch_collision<SID, ST, LGB_AA_ODD, MASKED, EXT>(coll, p, s);
+        break;
     case LGB_AA_UNPACK:
-        if constexpr (!MASKED) return dispatch_collision<SID, ST, LGB_AA_UNPACK, false, EXT>(coll, p, s);
-        return cudaErrorInvalidValue;
+        if constexpr (OTHER && !MASKED)
+            return dispatch_collision<SID, ST, LGB_AA_UNPACK, false, EXT>(coll, p, s);
+        break;
     }
     return cudaErrorInvalidValue;
 }
 
-// two translation units per (stencil, storage): lgb_step_<stencil>.cu built
+// translation units per (stencil, storage): lgb_step_<stencil>.cu built
 // with -DLGB_STORAGE_ID=<storage> and -DLGB_EXT_COLLISIONS=0 (step_*) or 1
-// (stepx_*)
+// (stepx_*), defining the entries for grids without boundaries (_plain) and
+// with them (_masked_pull: PULL and STREAM_ONLY; _masked_rest: the other
+// patterns), in one unit or three (-DLGB_MASK_PART)
+#define LGB_DECLARE_STEP_PART(name, part)                                                   \
+    cudaError_t name##_##part##_s0(int, int, const StepParams &, cudaStream_t);            \
+    cudaError_t name##_##part##_s1(int, int, const StepParams &, cudaStream_t);            \
+    cudaError_t name##_##part##_s2(int, int, const StepParams &, cudaStream_t);            \
+    cudaError_t name##_##part##_s3(int, int, const StepParams &, cudaStream_t);
 #define LGB_DECLARE_STEP(name)                                                              \
-    cudaError_t name##_s0(int, int, bool, const StepParams &, cudaStream_t);              \
-    cudaError_t name##_s1(int, int, bool, const StepParams &, cudaStream_t);              \
-    cudaError_t name##_s2(int, int, bool, const StepParams &, cudaStream_t);              \
-    cudaError_t name##_s3(int, int, bool, const StepParams &, cudaStream_t);
+    LGB_DECLARE_STEP_PART(name, plain)                                                      \
+    LGB_DECLARE_STEP_PART(name, masked_pull)                                                \
+    LGB_DECLARE_STEP_PART(name, masked_rest)
 LGB_DECLARE_STEP(step_d1q3)
 LGB_DECLARE_STEP(step_d2q9)
 LGB_DECLARE_STEP(step_d3q15)
