@@ -325,6 +325,72 @@ def time_kbc_obstacle(lt, torch, device, peak, g, steps, warmup,
     return out
 
 
+def sphere_link_distances(rows, centre, radius):
+    """wall distance of each link (q, x) of a sphere: the fraction t of e_q
+    from the fluid cell x to the surface, |x + t e_q - c| = r"""
+    import lettuce_gb300 as lt
+    e = np.asarray(lt.D3Q27().e, dtype=np.float64)[rows[:, 0]]
+    x = rows[:, 1:].astype(np.float64) - np.asarray(centre)
+    a = np.sum(e * e, axis=1)
+    b = 2.0 * np.sum(e * x, axis=1)
+    c = np.sum(x * x, axis=1) - radius * radius
+    t = (-b - np.sqrt(np.maximum(b * b - 4.0 * a * c, 0.0))) / (2.0 * a)
+    return np.clip(t, 1e-3, 1.0)
+
+
+def time_bounce_back_obstacle(lt, torch, device, peak, g, steps, warmup):
+    """config 3's obstacle with the sphere as one of the example project's
+    post-streaming boundaries instead of full-way bounce-back: halfway, and
+    linear interpolated with the sphere's wall distances, both computing
+    the momentum-exchange force every step (EbbSimulation: collide, stream,
+    bounce)"""
+    import math
+
+    class EbbObstacle(lt.Obstacle):
+        psb = ()
+
+        @property
+        def post_streaming_boundaries(self):
+            return list(self.psb)
+
+    res = [2 * g, g // 2, g // 2]
+    n = int(np.prod(res))
+    r = 12.0 * g / 256
+    centre = [g / 2, (res[1] - 1) / 2, (res[2] - 1) / 2]
+    grid = np.meshgrid(*[np.arange(k) for k in res], indexing="ij", sparse=True)
+    solid = sum((gi - ci) ** 2 for gi, ci in zip(grid, centre)) < r * r
+    st = lt.D3Q27()
+    rows = lt.hwbb_links(st.e, st.opposite, solid)
+    out = {"links": int(len(rows))}
+    for kind in ("halfway", "interpolated"):
+        flow = EbbObstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                           res[0] / (24 * g / 256), stencil=lt.D3Q27)
+        flow.initialize()
+        sbd = lt.SolidBoundaryData()
+        sbd.solid_mask = solid
+        if kind == "halfway":
+            b = lt.HalfwayBounceBackBoundary(flow.context, flow, sbd, calc_force=True)
+        else:
+            d = sphere_link_distances(rows, centre, r)
+            small = d < 0.5
+            sbd.f_index_lt, sbd.f_index_gt = rows[small], rows[~small]
+            sbd.d_lt, sbd.d_gt = d[small], d[~small]
+            b = lt.LinearInterpolatedBounceBackBoundary(flow.context, flow, sbd, calc_force=True)
+        flow.psb = [b]
+        sim = lt.EbbSimulation(flow, lt.KBCCollision(), [])
+        torch.cuda.nvtx.range_push("lgb_timed")
+        ms = _event_ms(torch, sim._collide_and_stream, steps, warmup, device)
+        torch.cuda.nvtx.range_pop()
+        force = b.force_sum.double().cpu().numpy()
+        gbs = 217 * n / (ms * 1e-3) / 1e9
+        out[kind] = {"mlups": round(n / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms, 4),
+                     "achieved_gbs": round(gbs, 1), "frac_of_peak": round(gbs / peak, 4),
+                     "force_x": round(float(force[0]), 6)}
+        del sim, flow, b
+        torch.cuda.empty_cache()
+    return out
+
+
 def measure_configs(lt, torch, device, peak):
     """the other configurations of the workload family, each at full size
     with a short timed run (CUDA events, inputs larger than L2):
@@ -341,6 +407,11 @@ def measure_configs(lt, torch, device, peak):
     c3 = {"workload": "D3Q27 KBC obstacle 512x128x128, float32", "bytes_per_cell": 217}
     c3.update(time_kbc_obstacle(lt, torch, device, peak, 256, 100, 10))
     out["config3_kbc_obstacle"] = c3
+    c3b = {"workload": "D3Q27 KBC obstacle 512x128x128, float32, sphere as the example "
+                       "project's halfway / interpolated bounce-back with its force",
+           "bytes_per_cell": 217}
+    c3b.update(time_bounce_back_obstacle(lt, torch, device, peak, 256, 100, 10))
+    out["config3_post_streaming_bounce_back"] = c3b
 
     c4 = {"workload": "256 D2Q9 TRT Taylor-Green domains, sides in [32, 512], Re in [100, 5000]"}
     for storage in (None, "fp16_shifted"):
