@@ -177,7 +177,15 @@ typedef struct {
     const uint32_t *force_links; /* [n_force_links][3] */
     int64_t n_force_links;
     double *force_out;
+    /* device scratch for the force's partial sums, float64
+     * [3 * ceil(n_force_links / LGB_LINK_FORCE_BLOCK)]; needed with
+     * force_out (the blocks' partial sums are added in a fixed order, so
+     * the force does not depend on scheduling) */
+    double *force_scratch;
 } lgb_step_desc;
+
+/* links per block of the momentum-exchange reduction */
+#define LGB_LINK_FORCE_BLOCK 256
 
 /* options: run the one-cell-per-thread kernel even where the two-cell
  * kernel of the 16-bit formats applies (results are bit-identical) */

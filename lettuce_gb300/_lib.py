@@ -13,6 +13,7 @@ import threading
 from . import build as _build
 
 ABI_VERSION = 3
+LINK_FORCE_BLOCK = 256  # LGB_LINK_FORCE_BLOCK
 MAX_SUBSTEPS = 8
 REDUCE_FIELDS = 5
 
@@ -79,7 +80,8 @@ class StepDesc(ctypes.Structure):
                 ("n_links", ctypes.c_int64),
                 ("force_links", ctypes.c_void_p),
                 ("n_force_links", ctypes.c_int64),
-                ("force_out", ctypes.c_void_p)]
+                ("force_out", ctypes.c_void_p),
+                ("force_scratch", ctypes.c_void_p)]
 
 
 class LibraryError(RuntimeError):

@@ -623,6 +623,10 @@ class EbbSimulation(Simulation):
             d.force_links = self._force_links.data_ptr() if len(trip) else None
             d.n_force_links = len(trip)
             d.force_out = psb[forcing[0]]._force.data_ptr()
+            blocks = -(-len(trip) // _lib.LINK_FORCE_BLOCK)
+            self._force_scratch = torch.zeros(3 * max(1, blocks), dtype=torch.float64,
+                                              device=dev)
+            d.force_scratch = self._force_scratch.data_ptr()
 
     def _choose_pull_post(self):
         if self._link_bits is not None:

@@ -416,62 +416,91 @@ cudaError_t launch_convert(int src_st, const void *src, int dst_st, void *dst, u
 // 211-218, linear_interpolated_bounce_back_boundary.py:104-126):
 // F = sum_k (g_k + b_k) e_{q_k}, g_k = f*_{q_k}(n_k) from the post-collision
 // field, b_k the bounced value (link_val[j_k], or g_k for a halfway link),
-// over the (q_k, n_k, j_k) triplets. One block, a fixed summation order:
-// the result does not depend on scheduling. Entries outside the field or
-// the value table are skipped.
+// over the (q_k, n_k, j_k) triplets. Block b reduces links
+// [b * 256, b * 256 + 256) into partial[3 b .. 3 b + 2] by a fixed tree;
+// link_force_total adds the partial sums in a fixed order, so the result
+// does not depend on scheduling. Entries outside the field or the value
+// table count zero.
 template <int SID, int ST>
-__global__ void __launch_bounds__(256) link_force_kernel(const void *f, uint64_t n_cells,
-                                                         const uint32_t *links, int64_t n_links,
-                                                         const void *vals, int64_t n_vals,
-                                                         double *out) {
+__global__ void __launch_bounds__(LGB_LINK_FORCE_BLOCK)
+link_force_partial(const void *f, uint64_t n_cells, const uint32_t *links, int64_t n_links,
+                   const void *vals, int64_t n_vals, double *partial) {
     using S = lgb::Stencil<SID>;
     using Sto = lgb::Storage<ST>;
-    __shared__ double part[3][256];
+    __shared__ double part[3][LGB_LINK_FORCE_BLOCK];
     double F[3] = {0.0, 0.0, 0.0};
-    for (int64_t k = threadIdx.x; k < n_links; k += blockDim.x) {
+    const int64_t k = blockIdx.x * (int64_t)LGB_LINK_FORCE_BLOCK + threadIdx.x;
+    if (k < n_links) {
         const uint32_t q = links[3 * k], n = links[3 * k + 1], j = links[3 * k + 2];
-        if (q >= (uint32_t)S::Q || (uint64_t)n >= n_cells) continue;
-        double w = 0.0;
-        int e[3] = {0, 0, 0};
+        bool ok = q < (uint32_t)S::Q && (uint64_t)n < n_cells;
+        if (j != 0xffffffffu && (!vals || (int64_t)j >= n_vals)) ok = false;
+        if (ok) {
+            double w = 0.0;
+            int e[3] = {0, 0, 0};
 #pragma unroll
-        for (int i = 0; i < S::Q; ++i) {
-            if ((uint32_t)i == q) {
-                w = S::w(i);
+            for (int i = 0; i < S::Q; ++i) {
+                if ((uint32_t)i == q) {
+                    w = S::w(i);
 #pragma unroll
-                for (int d = 0; d < S::D; ++d) e[d] = S::e(i, d);
+                    for (int d = 0; d < S::D; ++d) e[d] = S::e(i, d);
+                }
             }
-        }
-        const double v = (double)Sto::load_plain(
-            static_cast<const typename Sto::T *>(f) + (uint64_t)q * n_cells + n, w);
-        double b = v;
-        if (j != 0xffffffffu) {
-            if (!vals || (int64_t)j >= n_vals) continue;
-            b = (double)Sto::load_plain(static_cast<const typename Sto::T *>(vals) + j, w);
-        }
+            const double v = (double)Sto::load_plain(
+                static_cast<const typename Sto::T *>(f) + (uint64_t)q * n_cells + n, w);
+            const double b = j == 0xffffffffu
+                                 ? v
+                                 : (double)Sto::load_plain(
+                                       static_cast<const typename Sto::T *>(vals) + j, w);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) F[d] += (v + b) * (double)e[d];
+            for (int d = 0; d < 3; ++d) F[d] = (v + b) * (double)e[d];
+        }
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) part[d][threadIdx.x] = F[d];
     __syncthreads();
-    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    for (int h = LGB_LINK_FORCE_BLOCK / 2; h > 0; h >>= 1) {
         if ((int)threadIdx.x < h) {
 #pragma unroll
             for (int d = 0; d < 3; ++d) part[d][threadIdx.x] += part[d][threadIdx.x + h];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 3) partial[3 * blockIdx.x + threadIdx.x] = part[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(LGB_LINK_FORCE_BLOCK)
+link_force_total(const double *partial, int64_t n_blocks, double *out) {
+    __shared__ double part[3][LGB_LINK_FORCE_BLOCK];
+    double F[3] = {0.0, 0.0, 0.0};
+    for (int64_t b = threadIdx.x; b < n_blocks; b += LGB_LINK_FORCE_BLOCK) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) out[d] = part[d][0];
+        for (int d = 0; d < 3; ++d) F[d] += partial[3 * b + d];
     }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) part[d][threadIdx.x] = F[d];
+    __syncthreads();
+    for (int h = LGB_LINK_FORCE_BLOCK / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) part[d][threadIdx.x] += part[d][threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) out[threadIdx.x] = part[threadIdx.x][0];
 }
 
 template <int SID, int ST>
 cudaError_t launch_link_force_ss(const void *f, uint64_t n_cells, const uint32_t *links,
                                  int64_t n_links, const void *vals, int64_t n_vals, double *out,
-                                 cudaStream_t s) {
-    link_force_kernel<SID, ST><<<1, 256, 0, s>>>(f, n_cells, links, n_links, vals, n_vals, out);
+                                 double *scratch, cudaStream_t s) {
+    const int64_t blocks = (n_links + LGB_LINK_FORCE_BLOCK - 1) / LGB_LINK_FORCE_BLOCK;
+    if (blocks > 0) {
+        link_force_partial<SID, ST><<<(unsigned)blocks, LGB_LINK_FORCE_BLOCK, 0, s>>>(
+            f, n_cells, links, n_links, vals, n_vals, scratch);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    link_force_total<<<1, LGB_LINK_FORCE_BLOCK, 0, s>>>(scratch, blocks, out);
     return cudaGetLastError();
 }
 
@@ -549,8 +578,9 @@ cudaError_t launch_link_values_ss(const void *f, const Grid &g, const uint32_t *
 
 cudaError_t launch_link_force(int stencil, int storage, const void *f, uint64_t n_cells,
                               const uint32_t *links, int64_t n_links, const void *vals,
-                              int64_t n_vals, double *out, cudaStream_t s) {
-#define CALL(SID, ST) launch_link_force_ss<SID, ST>(f, n_cells, links, n_links, vals, n_vals, out, s)
+                              int64_t n_vals, double *out, double *scratch, cudaStream_t s) {
+#define CALL(SID, ST) \
+    launch_link_force_ss<SID, ST>(f, n_cells, links, n_links, vals, n_vals, out, scratch, s)
     LGB_SWITCH_SS(stencil, storage, CALL)
 #undef CALL
     return cudaErrorInvalidValue;
@@ -754,6 +784,10 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     if (d->force_out && (d->n_force_links < 0 || (d->n_force_links > 0 && !d->force_links)))
         return fail("lgb_step: %lld force links at %p", (long long)d->n_force_links,
                     (const void *)d->force_links);
+    if (d->force_out && !d->force_scratch)
+        return fail("lgb_step: force_out needs force_scratch");
+    if (d->force_out && d->n_force_links > 0xffffffffLL * LGB_LINK_FORCE_BLOCK)
+        return fail("lgb_step: %lld force links", (long long)d->n_force_links);
     const bool streams = d->pattern == LGB_PULL || d->pattern == LGB_STREAM_ONLY;
     if (p.link_val && streams) {
         // the interpolated values come from f_in before the step reads them
@@ -781,7 +815,7 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
         // f_in still holds the post-collision field the links bounced
         e = launch_link_force(d->stencil, d->storage, d->f_in, g.N, d->force_links,
                               d->n_force_links, d->link_val, d->n_links, d->force_out,
-                              static_cast<cudaStream_t>(stream));
+                              d->force_scratch, static_cast<cudaStream_t>(stream));
         if (e != cudaSuccess) return cuda_fail(e, "lgb_step: link force launch failed");
     }
     return 0;

@@ -126,6 +126,9 @@ def test_step_validation_masked(lgb):
                     (dict(force_links=0x6000), "without link_bits"),
                     (dict(flags=0x3000, n_sub=1, collision_index=0, link_bits=0x5000,
                           force_out=0x6000, n_force_links=4), "force links"),
+                    (dict(flags=0x3000, n_sub=1, collision_index=0, link_bits=0x5000,
+                          force_out=0x6000, force_links=0x7000, n_force_links=4),
+                     "force_scratch"),
                     (dict(link_val=0x6000), "without link_bits"),
                     (dict(flags=0x3000, n_sub=1, collision_index=0, link_bits=0x5000,
                           link_val=0x6000, link_base=0x7000, link_pairs=0x8000,
