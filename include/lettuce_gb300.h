@@ -169,7 +169,10 @@ typedef struct {
      * linear_interpolated_bounce_back_boundary.py:104-126): force_links
      * holds n_force_links triplets (q, n, k), q pointing from cell n into
      * the solid, k the link's index in link_val or 0xffffffff for a halfway
-     * link. LGB_PULL and LGB_STREAM_ONLY launches, whose stream crosses the
+     * link; k with bit 31 set marks a link of the post-streaming full-way
+     * bounce-back (fullway_bounce_back_boundary.py:137-178: a solid-cell
+     * link of distance 0, counted as 2 b e_q with b its streamed value,
+     * entry k & 0x7fffffff). LGB_PULL and LGB_STREAM_ONLY launches, whose stream crosses the
      * links, write sum (f*_q(n) + b) e_q, b = link_val[k] or f*_q(n)
      * (f* = the post-collision field f_in), to force_out (float64 [3],
      * lattice units, lettuce dimension order; unused trailing entries 0);

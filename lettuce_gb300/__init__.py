@@ -18,9 +18,9 @@ from ._collision import (BGKCollision, Collision, KBCCollision, MRTCollision, No
 from ._moments import D1Q3Transform, D2Q9Dellar, D2Q9Lallemand, D3Q27Hermite, Transform
 from ._force import Force, Guo, ShanChen
 from ._boundary import (AntiBounceBackOutlet, BounceBackBoundary, EquilibriumBoundaryPU,
-                        EquilibriumOutletP, HalfwayBounceBackBoundary,
-                        LinearInterpolatedBounceBackBoundary, PartiallySaturatedBC,
-                        SolidBoundaryData, hwbb_links)
+                        EquilibriumOutletP, FullwayBounceBackBoundary,
+                        HalfwayBounceBackBoundary, LinearInterpolatedBounceBackBoundary,
+                        PartiallySaturatedBC, SolidBoundaryData, fwbb_links, hwbb_links)
 from ._simulation import (BreakableSimulation, EbbSimulation, Reporter, Simulation,
                           StreamingStrategy)
 from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporterBase,
@@ -41,7 +41,7 @@ __all__ = [
     "TRTCollision", "KBCCollision", "NoCollision", "BounceBackBoundary",
     "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "EquilibriumOutletP",
     "PartiallySaturatedBC", "HalfwayBounceBackBoundary", "LinearInterpolatedBounceBackBoundary",
-    "SolidBoundaryData", "hwbb_links",
+    "FullwayBounceBackBoundary", "SolidBoundaryData", "hwbb_links", "fwbb_links",
     "Simulation", "EbbSimulation",
     "BreakableSimulation", "StreamingStrategy", "Reporter", "Observable",
     "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",

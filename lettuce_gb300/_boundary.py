@@ -6,12 +6,12 @@
 * EquilibriumOutletP -- lettuce/ext/_boundary/equilibrium_outlet_p.py:12-91
 * PartiallySaturatedBC -- lettuce/ext/_boundary/partially_saturated_boundary.py:6-51
 * HalfwayBounceBackBoundary, LinearInterpolatedBounceBackBoundary,
-  SolidBoundaryData -- lettuce's example project
+  FullwayBounceBackBoundary, SolidBoundaryData -- lettuce's example project
   examples/advanced_projects/efficient_bounce_back_obstacle/boundary/
   halfway_bounce_back_boundary.py:10-254,
-  linear_interpolated_bounce_back_boundary.py:9-212 and
-  solid_boundary_data.py:7-14; post-streaming boundaries, run by
-  ``EbbSimulation``
+  linear_interpolated_bounce_back_boundary.py:9-212,
+  fullway_bounce_back_boundary.py:9-185 and solid_boundary_data.py:7-14;
+  post-streaming boundaries, run by ``EbbSimulation``
 
 The masks are built exactly as lettuce builds them (they are combined by
 ``Simulation`` into the per-cell flag byte); the operators themselves run
@@ -32,7 +32,8 @@ from ._native import NativeBoundary, NativeCollision
 
 __all__ = ["BounceBackBoundary", "EquilibriumBoundaryPU", "AntiBounceBackOutlet",
            "EquilibriumOutletP", "PartiallySaturatedBC", "SolidBoundaryData",
-           "HalfwayBounceBackBoundary", "LinearInterpolatedBounceBackBoundary", "hwbb_links"]
+           "HalfwayBounceBackBoundary", "LinearInterpolatedBounceBackBoundary",
+           "FullwayBounceBackBoundary", "hwbb_links", "fwbb_links"]
 
 
 def _apply_alone(flow, native: NativeBoundary, flags_value):
@@ -253,6 +254,23 @@ def hwbb_links(e, opposite, mask, global_solid_mask=None, periodicity=None) -> n
     link (opposite[i], c)."""
     mask = _to_numpy_bool(mask)
     gmask = mask if global_solid_mask is None else _to_numpy_bool(global_solid_mask)
+    return _neighbour_links(e, opposite, mask, gmask, periodicity, at_solid=False)
+
+
+def fwbb_links(e, opposite, mask, global_solid_mask=None, periodicity=None) -> np.ndarray:
+    """The link list of the post-streaming full-way bounce-back's search
+    (fullway_bounce_back_boundary.py:47-131), rows (q, x, y[, z]) in its
+    order: the same neighbours c = p + e_i of the solid cells p as
+    ``hwbb_links``; a neighbour that is neither in ``mask`` nor in the
+    other solids of ``global_solid_mask`` (default: none) gives the link
+    (opposite[i], p), the population that streamed into the solid cell."""
+    mask = _to_numpy_bool(mask)
+    other = np.zeros_like(mask) if global_solid_mask is None else \
+        (_to_numpy_bool(global_solid_mask) & ~mask)
+    return _neighbour_links(e, opposite, mask, mask | other, periodicity, at_solid=True)
+
+
+def _neighbour_links(e, opposite, mask, gmask, periodicity, at_solid):
     e = np.asarray(e, dtype=np.int64)
     opp = np.asarray(opposite, dtype=np.int64)
     dims = mask.ndim
@@ -274,7 +292,8 @@ def hwbb_links(e, opposite, mask, global_solid_mask=None, periodicity=None) -> n
     idx = tuple(wrapped[..., k] for k in range(dims))
     ok &= ~mask[idx] & ~gmask[idx]
     q = np.broadcast_to(opp[None, :], ok.shape)
-    rows = np.concatenate([q[..., None], c], axis=-1)[ok]
+    at = np.broadcast_to(p[:, None, :], c.shape) if at_solid else c
+    rows = np.concatenate([q[..., None], at], axis=-1)[ok]
     return rows.reshape(-1, dims + 1).astype(np.int64)
 
 
@@ -412,6 +431,66 @@ class LinearInterpolatedBounceBackBoundary(Boundary):
 
     def make_no_streaming_mask(self, shape: List[int], context) -> torch.Tensor:
         return torch.as_tensor(self.mask, device=context.device)
+
+    def native_available(self) -> bool:
+        return True
+
+    def native_generator(self, index: int) -> NativeBoundary:
+        return NativeBoundary(_lib.SUB_NONE, index)
+
+
+class FullwayBounceBackBoundary(Boundary):
+    """The example project's post-streaming full-way bounce-back
+    (fullway_bounce_back_boundary.py:9-185), with momentum exchange. Its
+    solid cells do not collide but do stream; after each step's stream the
+    solid cell p sets population opp(q) to the population q that streamed
+    in from a fluid neighbour, for each link (q, p) of ``fwbb_links``. With
+    ``calc_force`` the momentum exchange 2 sum f_q(p) e_q over the links
+    (f_q(p) the streamed value) is kept as ``force_sum``. Runs inside the
+    step kernel's pull (``EbbSimulation``), as links of distance 0 of the
+    interpolated bounce-back's table, whose value is the streamed one. Not
+    lettuce's own ``BounceBackBoundary``, which replaces the collision."""
+
+    def __init__(self, context, flow, mask, global_solid_mask=None, periodicity=None,
+                 calc_force: bool = False):
+        self.context = context
+        self.flow = flow
+        self.mask = _to_numpy_bool(mask)
+        st = flow.stencil
+        if periodicity is None:
+            periodicity = (False, False, False if st.d == 3 else None)
+        rows = fwbb_links(st.e, st.opposite, self.mask, global_solid_mask,
+                          tuple(periodicity)[:st.d])
+        self.f_index_fwbb = torch.as_tensor(rows, dtype=torch.int64, device=context.device)
+        self.calc_force = bool(calc_force)
+        self._force = None
+        if self.calc_force:
+            self._force = torch.zeros(3, dtype=torch.float64, device=context.device)
+
+    @property
+    def force_sum(self) -> torch.Tensor:
+        """momentum-exchange force of the last step's links, [D], context
+        dtype (lattice units); reading it applies a pending stream"""
+        if self._force is None:
+            raise AttributeError("force_sum needs calc_force=True")
+        self.flow._settle()
+        return self._force[:self.flow.stencil.d].to(self.context.dtype)
+
+    def link_rows(self):
+        """(link rows q, x, y[, z] at the solid cells as int64 [K, 1 + D],
+        wall distances 0: the bounced value is the streamed one)"""
+        rows = self.f_index_fwbb.detach().cpu().numpy().astype(np.int64)
+        return rows, np.zeros(len(rows))
+
+    def __call__(self, flow):
+        raise RuntimeError("the post-streaming full-way bounce-back runs inside the step of "
+                           "an EbbSimulation")
+
+    def make_no_collision_mask(self, shape: List[int], context) -> torch.Tensor:
+        return torch.as_tensor(self.mask, device=context.device)
+
+    def make_no_streaming_mask(self, shape: List[int], context):
+        return None
 
     def native_available(self) -> bool:
         return True

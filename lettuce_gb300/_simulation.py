@@ -521,17 +521,22 @@ class EbbSimulation(Simulation):
     field is read; ``_stream()`` called directly bounces as well. The
     ``LinearInterpolatedBounceBackBoundary`` adds a pass over its links
     before each pulling launch that computes the interpolated values the
-    pull then reads. One post-streaming boundary may compute its force."""
+    pull then reads; the example's post-streaming
+    ``FullwayBounceBackBoundary`` runs as such links of distance 0 on its
+    solid cells (the bounced value is the streamed one). One
+    post-streaming boundary may compute its force."""
 
     def __init__(self, flow, collision, reporter: List[Reporter],
                  use_graph: Optional[bool] = None):
-        from ._boundary import HalfwayBounceBackBoundary, LinearInterpolatedBounceBackBoundary
+        from ._boundary import (FullwayBounceBackBoundary, HalfwayBounceBackBoundary,
+                                LinearInterpolatedBounceBackBoundary)
         psb = []
         if hasattr(flow.__class__, "post_streaming_boundaries"):
             psb = list(flow.post_streaming_boundaries or [])
         other = [b.__class__.__name__ for b in psb
                  if not isinstance(b, (HalfwayBounceBackBoundary,
-                                       LinearInterpolatedBounceBackBoundary))]
+                                       LinearInterpolatedBounceBackBoundary,
+                                       FullwayBounceBackBoundary))]
         if other:
             raise NotImplementedError(
                 f"no GB300 kernel for the post-streaming boundary {', '.join(other)}")
@@ -615,8 +620,11 @@ class EbbSimulation(Simulation):
             pos[order] = np.arange(len(order))
         forcing = [j for j, b in enumerate(psb) if b.calc_force]
         if forcing:
+            from ._boundary import FullwayBounceBackBoundary
             sel = owner == forcing[0]
             k = np.where(dist[sel] >= 0, pos[sel], 0xFFFFFFFF)
+            if isinstance(psb[forcing[0]], FullwayBounceBackBoundary):
+                k = k | 0x80000000  # 2 f_q e_q with f_q the streamed value
             trip = np.stack([q[sel], cells[sel], k], axis=1).astype(np.uint32)
             self._force_links = torch.as_tensor(np.ascontiguousarray(trip).view(np.int32),
                                                 device=dev)

@@ -416,7 +416,9 @@ cudaError_t launch_convert(int src_st, const void *src, int dst_st, void *dst, u
 // 211-218, linear_interpolated_bounce_back_boundary.py:104-126):
 // F = sum_k (g_k + b_k) e_{q_k}, g_k = f*_{q_k}(n_k) from the post-collision
 // field, b_k the bounced value (link_val[j_k], or g_k for a halfway link),
-// over the (q_k, n_k, j_k) triplets. Block b reduces links
+// over the (q_k, n_k, j_k) triplets; a full-way link (bit 31 of j_k) counts
+// 2 b_k e_{q_k}, b_k its streamed value (fullway_bounce_back_boundary.py:
+// 163-178). Block b reduces links
 // [b * 256, b * 256 + 256) into partial[3 b .. 3 b + 2] by a fixed tree;
 // link_force_total adds the partial sums in a fixed order, so the result
 // does not depend on scheduling. Entries outside the field or the value
@@ -431,9 +433,14 @@ link_force_partial(const void *f, uint64_t n_cells, const uint32_t *links, int64
     double F[3] = {0.0, 0.0, 0.0};
     const int64_t k = blockIdx.x * (int64_t)LGB_LINK_FORCE_BLOCK + threadIdx.x;
     if (k < n_links) {
-        const uint32_t q = links[3 * k], n = links[3 * k + 1], j = links[3 * k + 2];
+        const uint32_t q = links[3 * k], n = links[3 * k + 1], jj = links[3 * k + 2];
+        // jj: 0xffffffff = halfway; bit 31 set = full-way (2 b e_q, b the
+        // streamed value in entry jj & 0x7fffffff); else interpolated
+        const bool halfway = jj == 0xffffffffu;
+        const bool fullway = !halfway && (jj & 0x80000000u);
+        const uint32_t j = jj & 0x7fffffffu;
         bool ok = q < (uint32_t)S::Q && (uint64_t)n < n_cells;
-        if (j != 0xffffffffu && (!vals || (int64_t)j >= n_vals)) ok = false;
+        if (!halfway && (!vals || (int64_t)j >= n_vals)) ok = false;
         if (ok) {
             double w = 0.0;
             int e[3] = {0, 0, 0};
@@ -447,12 +454,12 @@ link_force_partial(const void *f, uint64_t n_cells, const uint32_t *links, int64
             }
             const double v = (double)Sto::load_plain(
                 static_cast<const typename Sto::T *>(f) + (uint64_t)q * n_cells + n, w);
-            const double b = j == 0xffffffffu
-                                 ? v
-                                 : (double)Sto::load_plain(
-                                       static_cast<const typename Sto::T *>(vals) + j, w);
+            const double b = halfway ? v
+                                     : (double)Sto::load_plain(
+                                           static_cast<const typename Sto::T *>(vals) + j, w);
+            const double m = fullway ? 2.0 * b : v + b;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) F[d] = (v + b) * (double)e[d];
+            for (int d = 0; d < 3; ++d) F[d] = m * (double)e[d];
         }
     }
 #pragma unroll

@@ -33,6 +33,8 @@
  *                   simulation/ebb_simulation.py:72-101
  *   interpolated bounce-back (same project)
  *                   boundary/linear_interpolated_bounce_back_boundary.py:55-153
+ *   post-streaming full-way bounce-back (same project)
+ *                   boundary/fullway_bounce_back_boundary.py:137-178
  *
  * Parity of this restatement with lettuce itself is pinned by golden
  * vectors generated from lettuce (tests/golden/make_golden.py).
@@ -116,7 +118,11 @@ typedef struct {
      * read the field before any is bounced. The force of a step is
      * sum_k (g_k + bounced_k) e_{q_k} (2 g_k e_{q_k} for a halfway link). */
     const double *link_d;
-    const uint8_t *link_force; /* [n_links] 1 = counted in force_out; NULL = all */
+    /* [n_links] how a link counts in force_out: 0 not, 1 (g + bounced) e_q,
+     * 2 2 f_q(n) e_q with f_q(n) the streamed value (the post-streaming
+     * full-way bounce-back, whose links sit on solid cells and use
+     * d = 0); NULL = all 1 */
+    const uint8_t *link_force;
 } orc_problem;
 
 int orc_stencil_dq(int stencil, int *d, int *q);

@@ -540,9 +540,11 @@ static int SFX(orc_run_impl)(const orc_problem *p, REAL *f, REAL *work, int nste
             for (int64_t k = 0; k < K; ++k) {
                 const int q = (int)p->links[2 * k];
                 cur[(int64_t)g.st->opp[q] * g.N + p->links[2 * k + 1]] = val[k];
-                if (p->link_force && !p->link_force[k]) continue;
-                for (int d = 0; d < g.d; ++d)
-                    force[d] += ((double)fcol[k] + (double)val[k]) * g.st->e[q][d];
+                const int mode = p->link_force ? p->link_force[k] : 1;
+                const double gb = mode == 2 ? 2.0 * (double)val[k]
+                                            : (double)fcol[k] + (double)val[k];
+                if (mode == 0) continue;
+                for (int d = 0; d < g.d; ++d) force[d] += gb * g.st->e[q][d];
             }
             if (p->force_out)
                 for (int d = 0; d < 3; ++d) p->force_out[3 * s + d] = force[d];

@@ -220,7 +220,8 @@ def ebb_masks(resolution, q, name, pre, post, post_streaming):
     ebb_simulation.py:28-57): lettuce's masks, created filled with the
     collision index if there were none, then each post-streaming
     boundary's solid cells take index collision_index + 1 + len(post) + j
-    and keep all populations in the stream"""
+    and, except for the full-way variant's, keep all populations in the
+    stream"""
     ncm, nsm = assemble_masks(resolution, q, name, pre, post)
     if not post_streaming:
         return ncm, nsm
@@ -231,7 +232,10 @@ def ebb_masks(resolution, q, name, pre, post, post_streaming):
     for i, b in enumerate(post_streaming, start=ci + 1 + len(post)):
         solid = np.asarray(b["solid"], dtype=bool)
         ncm[solid] = i
-        nsm |= solid[None].astype(np.uint8)
+        if not b.get("fullway"):
+            # the full-way variant's solid cells stream
+            # (fullway_bounce_back_boundary.py:182-184)
+            nsm |= solid[None].astype(np.uint8)
     return ncm, nsm
 
 
@@ -259,7 +263,9 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
     project, dicts with "solid" (mask), "f_index" (link rows q, x, y[, z])
     and, for the linear interpolated one, "d" (wall distance per row;
     without it the links are halfway), "force" (default True: its links
-    count into ``forces``); with any, every step runs collide,
+    count into ``forces``); the post-streaming full-way bounce-back is
+    "fullway": True with its solid-cell links and d = 0 (the bounced value
+    is then the streamed one); with any, every step runs collide,
     stream, bounce (the example EbbSimulation) whatever ``strategy`` says,
     and ``forces`` (float64 [nsteps, 3], optional) receives each step's
     momentum-exchange force over all links."""
@@ -342,7 +348,8 @@ def run(name, f, nsteps, collision="bgk", tau=1.0, tau_minus=1.0,
              for b in post_streaming]))
         counted = np.ascontiguousarray(np.concatenate(
             [np.full(len(np.asarray(b["f_index"]).reshape(-1, len(res) + 1)),
-                     1 if b.get("force", True) else 0, dtype=np.uint8)
+                     0 if not b.get("force", True) else (2 if b.get("fullway") else 1),
+                     dtype=np.uint8)
              for b in post_streaming]))
         keep += [links, dist, counted]
         p.n_links = len(links)

@@ -586,6 +586,72 @@ def ibb_cases():
              periodicity=(False, True, True))
 
 
+def case_fwbb(name, stencil, res, coll, steps, seed, solid, periodicity=None,
+              global_extra=None):
+    """lettuce's example post-streaming full-way bounce-back
+    (examples/advanced_projects/efficient_bounce_back_obstacle/boundary/
+    fullway_bounce_back_boundary.py) under the example's EbbSimulation, with
+    its momentum-exchange force after every step; ``global_extra`` is a
+    second solid region given through ``global_solid_mask``."""
+    import lettuce
+    root = os.path.dirname(os.path.dirname(os.path.abspath(lettuce.__file__)))
+    for sub in ("boundary", "simulation"):
+        d = os.path.join(root, EBB, sub)
+        if d not in sys.path:
+            sys.path.insert(0, d)
+    from fullway_bounce_back_boundary import FullwayBounceBackBoundary
+    from ebb_simulation import EbbSimulation
+
+    class FwbbFlow(GivenFlow):
+        psb = []
+
+        @property
+        def post_streaming_boundaries(self):
+            return self.psb
+
+    st = stencil()
+    rng = np.random.default_rng(seed)
+    w = np.array(st.w).reshape([-1] + [1] * len(res))
+    f0 = w * (1.0 + 0.2 * rng.standard_normal([st.q] + res))
+    flow = FwbbFlow(st, f0)
+    gmask = None if global_extra is None else (solid | global_extra)
+    fw = FullwayBounceBackBoundary(CTX, flow, solid, global_solid_mask=gmask,
+                                   periodicity=periodicity, calc_force=True)
+    flow.psb = [fw]
+    tau = 0.8
+    sim = EbbSimulation(flow, collision_of(coll, tau), [])
+    out = {"f0": f0, "solid": solid, "tau": np.float64(tau), "steps": np.int64(steps),
+           "f_index": npf(fw.f_index_fwbb).astype(np.int64),
+           "ncm": npf(sim.no_collision_mask).astype(np.uint8),
+           "nsm": npf(sim.no_streaming_mask).astype(np.uint8)}
+    if global_extra is not None:
+        out["global_extra"] = global_extra
+    forces = []
+    for _ in range(steps):
+        sim(1)
+        forces.append(npf(fw.force_sum))
+    out["force"] = np.array(forces)
+    out["f"] = npf(flow.f)
+    out["meta"] = json.dumps({"stencil": stencil.__name__, "res": res, "collision": coll,
+                              "periodicity": None if periodicity is None else list(periodicity),
+                              "inlet": False})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
+def fwbb_cases():
+    g = np.meshgrid(np.arange(22), np.arange(12), indexing="ij")
+    solid = (g[0] - 9.0) ** 2 + (g[1] - 5.5) ** 2 < 3.3 ** 2
+    solid[0, 2:4] = True
+    solid[21, 7:9] = True
+    case_fwbb("fwbb_d2q9_bgk", D2Q9, [22, 12], "bgk", 6, 95, solid)
+    solid = np.zeros([9, 7, 6], dtype=bool)
+    solid[2:5, 2:5, 1:4] = True
+    extra = np.zeros_like(solid)
+    extra[5:7, 2:4, 1:3] = True
+    case_fwbb("fwbb_d3q19_trt", D3Q19, [9, 7, 6], "trt", 4, 96, solid,
+              periodicity=(False, True, True), global_extra=extra)
+
+
 def hwbb_cases():
     # a disc inside a non-periodic 2-D box, and two blocks on the x = 0 and
     # x = 23 columns: the neighbour search wraps negative indices (Python
@@ -618,6 +684,9 @@ def main():
         return
     if "--only-ibb" in sys.argv:
         ibb_cases()
+        return
+    if "--only-fwbb" in sys.argv:
+        fwbb_cases()
         return
     case_tgv("tgv2d_d2q9_bgk", D2Q9, 16, 1000, "bgk", 5)
     case_tgv("tgv2d_d2q9_trt", D2Q9, [16, 12], 300, "trt", 5)
@@ -656,6 +725,7 @@ def main():
     case_dump()
     hwbb_cases()
     ibb_cases()
+    fwbb_cases()
     case_native_kats()
     case_observables()
     case_adjoint()

@@ -124,3 +124,17 @@ def ibb_case(context, z, meta, f0=None):
     b = lt.LinearInterpolatedBounceBackBoundary(context, flow, sbd, calc_force=True)
     flow.psb = [b]
     return flow, b
+
+
+def fwbb_case(context, z, meta, f0=None):
+    """(flow, boundary) of a post-streaming full-way bounce-back golden case"""
+    stencil = getattr(lt, meta["stencil"])()
+    f0 = z["f0"] if f0 is None else f0
+    flow = HwbbFlow(context, stencil, f0)
+    g = None if "global_extra" not in z else (z["solid"] | z["global_extra"])
+    per = meta["periodicity"]
+    b = lt.FullwayBounceBackBoundary(context, flow, z["solid"], global_solid_mask=g,
+                                     periodicity=None if per is None else tuple(per),
+                                     calc_force=True)
+    flow.psb = [b]
+    return flow, b

@@ -212,3 +212,52 @@ def test_halfway_and_interpolated_together(lgb, oracle):
     np.testing.assert_allclose(to_np(flow.f), ref, rtol=0, atol=1e-13)
     np.testing.assert_allclose(to_np(ib.force_sum), forces[-1, :2], rtol=0, atol=1e-12)
     assert sim.status == 0
+
+
+# -- the post-streaming full-way bounce-back of the same project -------------
+
+FWBB_CASES = golden_names("fwbb_")
+
+
+def _fwbb_sim(z, m, dtype=torch.float64, storage=None, use_graph=False, f0=None):
+    from lgb_helpers import fwbb_case
+    ctx = lt.Context("cuda:0", dtype, storage=storage)
+    flow, b = fwbb_case(ctx, z, m, f0=f0)
+    coll = lt.TRTCollision(float(z["tau"]), 1.0) if m["collision"] == "trt" else \
+        lt.BGKCollision(float(z["tau"]))
+    return lt.EbbSimulation(flow, coll, [], use_graph=use_graph), flow, b
+
+
+@pytest.mark.parametrize("name", FWBB_CASES)
+def test_fwbb_f64_matches_example(lgb, name):
+    z = golden(name)
+    m = meta(z)
+    sim, flow, b = _fwbb_sim(z, m)
+    forces = []
+    for _ in range(int(z["steps"])):
+        sim(1)
+        forces.append(to_np(b.force_sum))
+    np.testing.assert_allclose(to_np(flow.f), z["f"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(np.array(forces), z["force"], rtol=0, atol=1e-12)
+    sim2, flow2, b2 = _fwbb_sim(z, m, use_graph=True)
+    sim2(int(z["steps"]))
+    np.testing.assert_allclose(to_np(flow2.f), z["f"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(to_np(b2.force_sum), z["force"][-1], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("storage,tol", [(None, 2e-6), ("fp16_shifted", 2e-3)])
+def test_fwbb_reduced_precision_against_oracle(lgb, oracle, storage, tol):
+    z = golden("fwbb_d3q19_trt")
+    m = meta(z)
+    steps = 10
+    forces = np.zeros((steps, 3))
+    ref = oracle.run(m["stencil"], z["f0"].astype(np.float32), steps, collision="trt",
+                     tau=float(z["tau"]), tau_minus=1.0,
+                     post_streaming=[dict(solid=z["solid"], f_index=z["f_index"],
+                                          d=np.zeros(len(z["f_index"])), fullway=True)],
+                     forces=forces)
+    sim, flow, b = _fwbb_sim(z, m, torch.float32, storage, use_graph=True,
+                             f0=z["f0"].astype(np.float32))
+    sim(steps)
+    assert rel_max(to_np(flow.f), ref) < tol
+    assert rel_max(to_np(b.force_sum), forces[-1]) < 50 * tol

@@ -1,5 +1,5 @@
-"""Halfway and linear interpolated bounce-back of lettuce's example project
-(the post-streaming boundaries of
+"""Halfway, linear interpolated and full-way bounce-back of lettuce's
+example project (the post-streaming boundaries of
 examples/advanced_projects/efficient_bounce_back_obstacle), on CPU: the oracle against the golden vectors the example itself produced
 (populations after every step's collide, stream, bounce, and the
 momentum-exchange force of each step), the product's neighbour search
@@ -11,10 +11,11 @@ import torch
 
 import lettuce_gb300 as lt
 from conftest import golden, golden_names, meta
-from lgb_helpers import hwbb_case, ibb_case
+from lgb_helpers import fwbb_case, hwbb_case, ibb_case
 
 CASES = golden_names("hwbb_")
 IBB_CASES = golden_names("ibb_")
+FWBB_CASES = golden_names("fwbb_")
 
 
 def _post(z, m):
@@ -184,3 +185,55 @@ def test_ibb_value_table_on_cpu(name):
     trip = sim._force_links.numpy().view(np.uint32)
     assert np.array_equal(pairs[trip[:, 2]], trip[:, :2])
     assert sim._link_val.dtype == flow.context.storage_dtype and len(sim._link_val) == len(rows)
+
+
+def _fw_post(z):
+    return [dict(solid=z["solid"], f_index=z["f_index"], d=np.zeros(len(z["f_index"])),
+                 fullway=True)]
+
+
+def test_fwbb_cases_present():
+    assert len(FWBB_CASES) == 2
+
+
+@pytest.mark.parametrize("name", FWBB_CASES)
+def test_oracle_matches_example_fullway(oracle, name):
+    z = golden(name)
+    m = meta(z)
+    steps = int(z["steps"])
+    forces = np.zeros((steps, 3))
+    out = oracle.run(m["stencil"], z["f0"], steps, collision=m["collision"],
+                     tau=float(z["tau"]), tau_minus=1.0, post_streaming=_fw_post(z),
+                     forces=forces)
+    np.testing.assert_allclose(out, z["f"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(forces[:, :len(m["res"])], z["force"], rtol=0, atol=1e-13)
+    ncm, nsm = oracle.ebb_masks(list(m["res"]), z["f0"].shape[0], m["stencil"], [], [],
+                                _fw_post(z))
+    assert np.array_equal(ncm, z["ncm"]) and np.array_equal(nsm, z["nsm"])
+
+
+@pytest.mark.parametrize("name", FWBB_CASES)
+def test_fullway_search_and_table_on_cpu(name):
+    """the solid-cell links reproduce the example's list row for row; in
+    the table they are distance-0 entries whose force triplets carry bit 31"""
+    z = golden(name)
+    m = meta(z)
+    st = getattr(lt, m["stencil"])()
+    per = m["periodicity"]
+    g = None if "global_extra" not in z else (z["solid"] | z["global_extra"])
+    rows = lt.fwbb_links(st.e, st.opposite, z["solid"], g,
+                         None if per is None else tuple(per)[:st.d])
+    assert np.array_equal(rows, z["f_index"])
+    flow, b = fwbb_case(lt.Context("cpu", torch.float64), z, m)
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.8), [])
+    assert np.array_equal(sim.no_collision_mask.numpy(), z["ncm"])
+    assert np.array_equal(sim.no_streaming_mask.numpy(), z["nsm"])
+    assert sim._nsb is None                     # the solid cells stream
+    bits = sim._link_bits.numpy().reshape(-1).view(np.uint32)
+    solid = np.asarray(z["solid"]).reshape(-1)
+    assert np.all(solid[bits != 0])             # the links sit on solid cells
+    assert np.all(sim._link_d.numpy() == 0)
+    trip = sim._force_links.numpy().view(np.uint32)
+    assert np.all(trip[:, 2] & 0x80000000)
+    pairs = sim._link_pairs.numpy().view(np.uint32)
+    assert np.array_equal(pairs[trip[:, 2] & 0x7FFFFFFF], trip[:, :2])
