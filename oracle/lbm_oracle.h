@@ -3,7 +3,8 @@
  *
  * A plain-C restatement of lettuce's torch step (stream by periodic roll,
  * masked collide substeps, boundary operators), used by the test-suite as
- * the checker and by bench.py as the timed CPU baseline. Nothing in the
+ * the reference of its comparisons and by bench.py as the timed CPU
+ * baseline. Nothing in the
  * product (lettuce_gb300/) links, loads or calls it.
  *
  * Each routine cites the lettuce source it restates (paths are relative to

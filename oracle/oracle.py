@@ -3,8 +3,8 @@
 Python face of ``oracle/lbm_oracle.c``: a restatement of lettuce's torch step
 (stream by periodic roll, masked collide substeps, boundary operators) in
 plain C. Only the test-suite, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` use this module, always as the checker or the timed CPU
-baseline, never as part of the product path.
+leg of ``bench.py`` use this module, always as the reference of a comparison
+or the timed CPU baseline, never as part of the product path.
 
 Boundaries are described by plain dicts so the oracle does not depend on the
 product's classes:
