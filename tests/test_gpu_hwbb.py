@@ -261,3 +261,53 @@ def test_fwbb_reduced_precision_against_oracle(lgb, oracle, storage, tol):
     sim(steps)
     assert rel_max(to_np(flow.f), ref) < tol
     assert rel_max(to_np(b.force_sum), forces[-1]) < 50 * tol
+
+
+# -- links next to the anti-bounce-back outlet --------------------------------
+
+@pytest.mark.parametrize("stencil,res,coll", [("D2Q9", [20, 10], "bgk"),
+                                              ("D3Q27", [14, 6, 6], "kbc")])
+def test_links_beside_the_outlet_against_oracle(lgb, oracle, stencil, res, coll):
+    """an equilibrium inlet, an anti-bounce-back outlet and a halfway
+    solid whose links sit on the outlet's neighbour plane and on the outlet
+    plane itself (the outlet's velocity extrapolation reads bounced cells;
+    the outlet-plane launch carries links), float64, against the oracle"""
+    from lgb_helpers import HwbbFlow
+    st = getattr(lt, stencil)()
+    d = len(res)
+    rng = np.random.default_rng(11)
+    w = np.asarray(st.w).reshape([-1] + [1] * d)
+    f0 = w * (1.0 + 0.05 * rng.standard_normal([st.q] + res))
+    X = res[0]
+    solid = np.zeros(res, dtype=bool)
+    solid[X - 4:X - 2, 2:4] = True      # its links reach x = X - 2
+    solid[X - 2, res[1] - 2] = True     # a solid cell on the neighbour plane
+    inlet = np.zeros(res, dtype=bool)
+    inlet[0] = True
+    ctx = lt.Context("cuda:0", torch.float64)
+    flow = HwbbFlow(ctx, st, f0)
+    vel = torch.tensor([0.02] + [0.0] * (d - 1), dtype=torch.float64)
+    eq = lt.EquilibriumBoundaryPU(ctx, flow, torch.as_tensor(inlet), vel)
+    flow._bnds = [eq, lt.AntiBounceBackOutlet([1] + [0] * (d - 1), flow)]
+    sbd = lt.SolidBoundaryData()
+    sbd.solid_mask = solid
+    hw = lt.HalfwayBounceBackBoundary(ctx, flow, sbd, calc_force=True)
+    assert np.any(hw.f_index.cpu().numpy()[:, 1] == X - 1)   # links on the outlet plane
+    flow.psb = [hw]
+    coll_obj = lt.KBCCollision(flow.units.relaxation_parameter_lu) if coll == "kbc" \
+        else lt.BGKCollision(0.7)
+    tau = flow.units.relaxation_parameter_lu if coll == "kbc" else 0.7
+    sim = lt.EbbSimulation(flow, coll_obj, [], use_graph=True)
+    steps = 7
+    sim(steps)
+    nat = eq.native_generator(1)
+    post = [{"kind": "equilibrium_pu", "mask": inlet,
+             "rho": nat.rho.cpu().numpy().reshape([1] * d),
+             "u": nat.u.cpu().numpy().reshape([d] + [1] * d)},
+            {"kind": "anti_bounce_back", "direction": [1] + [0] * (d - 1)}]
+    forces = np.zeros((steps, 3))
+    ref = oracle.run(stencil, f0, steps, collision=coll, tau=tau, post=post,
+                     post_streaming=[dict(solid=solid, f_index=hw.f_index.cpu().numpy())],
+                     forces=forces)
+    assert rel_max(to_np(flow.f), ref) < 1e-12
+    np.testing.assert_allclose(to_np(hw.force_sum), forces[-1, :d], rtol=1e-10, atol=1e-13)
