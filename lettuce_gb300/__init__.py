@@ -25,6 +25,7 @@ from ._simulation import (BreakableSimulation, EbbSimulation, Reporter, Simulati
                           StreamingStrategy)
 from ._reporter import (EnergySpectrum, Enstrophy, ErrorReporter, FailureReporterBase,
                         HighMaReporter, IncompressibleKineticEnergy, Mass,
+                        DragCoefficient, LiftCoefficient,
                         MaximumVelocity, NaNReporter, Observable, ObservableReporter)
 from ._flows import ExtFlow, Obstacle, PoiseuilleFlow2D, TaylorGreenVortex
 from ._native import NativeBoundary, NativeCollision, NativeEquilibrium
@@ -45,7 +46,8 @@ __all__ = [
     "Simulation", "EbbSimulation",
     "BreakableSimulation", "StreamingStrategy", "Reporter", "Observable",
     "ObservableReporter", "MaximumVelocity", "IncompressibleKineticEnergy",
-    "Enstrophy", "EnergySpectrum", "Mass", "ErrorReporter", "FailureReporterBase",
+    "Enstrophy", "EnergySpectrum", "Mass", "DragCoefficient", "LiftCoefficient",
+    "ErrorReporter", "FailureReporterBase",
     "NaNReporter", "HighMaReporter", "ExtFlow", "TaylorGreenVortex", "Obstacle",
     "NativeBoundary", "NativeCollision", "NativeEquilibrium", "BatchedSimulation",
     "batched_taylor_green", "rollout", "moments_torch", "Slab", "SlabSimulation",

@@ -21,6 +21,7 @@ from ._simulation import Reporter
 
 __all__ = ["Observable", "ObservableReporter", "MaximumVelocity",
            "IncompressibleKineticEnergy", "Enstrophy", "EnergySpectrum", "Mass",
+           "DragCoefficient", "LiftCoefficient",
            "ErrorReporter", "FailureReporterBase", "NaNReporter", "HighMaReporter",
            "reduce_flow"]
 
@@ -133,6 +134,42 @@ class Mass(Observable):
         if self.mask is not None:
             mass = mass - reduce_flow(self.flow, mask=self.mask)[4]
         return mass
+
+
+class DragCoefficient(Observable):
+    """Drag coefficient of an obstacle from its bounce-back boundary's
+    momentum exchange (the efficient-bounce-back example's
+    reporter/observables_force_coefficients.py:15-48):
+    F_x / (0.5 rho_mean u_lu^2 A_lu), with rho_mean the mean density over
+    the cells outside ``solid_mask`` (a float64 device reduction), u_lu the
+    characteristic velocity and A_lu = area_pu (L_lu / L_pu)^(D-1). The
+    boundary must compute its force (``calc_force=True``)."""
+    _axis = 0
+
+    def __init__(self, flow, obstacle_boundary, solid_mask, area_pu: float):
+        super().__init__(flow)
+        self.obstacle_boundary = obstacle_boundary
+        self.solid_mask = torch.as_tensor(np.asarray(solid_mask, dtype=bool)
+                                          if not isinstance(solid_mask, torch.Tensor)
+                                          else solid_mask, device=flow.context.device).bool()
+        self._fluid = (~self.solid_mask).to(torch.uint8).contiguous()
+        self._n_fluid = int(self._fluid.sum().item())
+        u = flow.units
+        self.area_lu = area_pu * (u.characteristic_length_lu /
+                                  u.characteristic_length_pu) ** (flow.stencil.d - 1)
+
+    def __call__(self, f: Optional[torch.Tensor] = None):
+        force = self.obstacle_boundary.force_sum[self._axis].double()
+        rho_mean = reduce_flow(self.flow, mask=self._fluid)[4] / max(1, self._n_fluid)
+        c = force / (0.5 * rho_mean * self.flow.units.characteristic_velocity_lu ** 2
+                     * self.area_lu)
+        return c.to(self.context.dtype)
+
+
+class LiftCoefficient(DragCoefficient):
+    """Lift coefficient: as ``DragCoefficient`` with the force along y
+    (observables_force_coefficients.py:51-83)"""
+    _axis = 1
 
 
 class ObservableReporter(Reporter):

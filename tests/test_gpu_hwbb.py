@@ -311,3 +311,29 @@ def test_links_beside_the_outlet_against_oracle(lgb, oracle, stencil, res, coll)
                      forces=forces)
     assert rel_max(to_np(flow.f), ref) < 1e-12
     np.testing.assert_allclose(to_np(hw.force_sum), forces[-1, :d], rtol=1e-10, atol=1e-13)
+
+
+def test_drag_and_lift_coefficients(lgb):
+    """the example's force coefficients from the halfway boundary's force
+    and the mean fluid density, against the same formula on the example's
+    own populations and force"""
+    z = golden("hwbb_d2q9_bgk")
+    m = meta(z)
+    sim, flow, hw = _sim(z, m, use_graph=True)
+    area_pu = 0.7
+    cd = lt.DragCoefficient(flow, hw, z["solid"], area_pu)
+    cl = lt.LiftCoefficient(flow, hw, z["solid"], area_pu)
+    sim(int(z["steps"]))
+    st = lt.D2Q9()
+    rho = z["f"].sum(axis=0)
+    rho_mean = rho[~z["solid"]].mean()
+    u = flow.units
+    area_lu = area_pu * (u.characteristic_length_lu / u.characteristic_length_pu)
+    denom = 0.5 * rho_mean * u.characteristic_velocity_lu ** 2 * area_lu
+    assert abs(cd().item() - z["force"][-1][0] / denom) < 1e-10 * abs(z["force"][-1][0] / denom)
+    assert abs(cl().item() - z["force"][-1][1] / denom) < 1e-9 * abs(z["force"][-1][1] / denom) + 1e-14
+    # as a reporter's observable
+    rep = lt.ObservableReporter(cd, interval=2, out=None)
+    sim.reporter.append(rep)
+    sim(2)
+    assert len(rep.out) >= 1 and np.isfinite(np.asarray(rep.out[-1][-1], dtype=float)).all()
