@@ -237,3 +237,48 @@ def test_fullway_search_and_table_on_cpu(name):
     assert np.all(trip[:, 2] & 0x80000000)
     pairs = sim._link_pairs.numpy().view(np.uint32)
     assert np.array_equal(pairs[trip[:, 2] & 0x7FFFFFFF], trip[:, :2])
+
+
+def _loop_search(e, opp, mask, other, periodicity, at_solid):
+    """the example's neighbour search written as its loops
+    (halfway_bounce_back_boundary.py:70-161, fullway_bounce_back_boundary.py:
+    47-131): border shifts on periodic axes, Python indexing (negative
+    indices wrap, past-the-end ones raise and drop the link)"""
+    rows = []
+    shape = mask.shape
+    for p in zip(*np.nonzero(mask)):
+        for i in range(len(e)):
+            border = [0] * mask.ndim
+            for k in range(mask.ndim):
+                if p[k] == 0 and e[i][k] == -1 and periodicity[k]:
+                    border[k] = -1
+                elif p[k] == shape[k] - 1 and e[i][k] == 1 and periodicity[k]:
+                    border[k] = 1
+            c = tuple(int(p[k] + e[i][k] - border[k] * shape[k]) for k in range(mask.ndim))
+            try:
+                hit = (not mask[c]) and (not other[c])
+            except IndexError:
+                continue
+            if hit:
+                rows.append([opp[i]] + (list(map(int, p)) if at_solid else list(c)))
+    return np.array(rows, dtype=np.int64).reshape(-1, mask.ndim + 1)
+
+
+@pytest.mark.parametrize("stencil,shape", [("D2Q9", (9, 7)), ("D3Q19", (6, 5, 4)),
+                                           ("D3Q27", (5, 5, 4))])
+def test_link_searches_equal_the_loops(stencil, shape):
+    import itertools
+    st = getattr(lt, stencil)()
+    rng = np.random.default_rng(sum(shape))
+    for trial, per in enumerate(itertools.product([False, True], repeat=len(shape))):
+        mask = rng.random(shape) < 0.25
+        extra = (rng.random(shape) < 0.15) & ~mask
+        glob = mask | extra
+        want = _loop_search(st.e, st.opposite, mask, glob, per, at_solid=False)
+        assert np.array_equal(lt.hwbb_links(st.e, st.opposite, mask, glob, per), want)
+        want = _loop_search(st.e, st.opposite, mask, mask, per, at_solid=False)
+        assert np.array_equal(lt.hwbb_links(st.e, st.opposite, mask, None, per), want)
+        want = _loop_search(st.e, st.opposite, mask, extra, per, at_solid=True)
+        assert np.array_equal(lt.fwbb_links(st.e, st.opposite, mask, glob, per), want)
+        want = _loop_search(st.e, st.opposite, mask, np.zeros_like(mask), per, at_solid=True)
+        assert np.array_equal(lt.fwbb_links(st.e, st.opposite, mask, None, per), want)
