@@ -12,6 +12,7 @@ from ._context import Context
 from ._stencil import D1Q3, D2Q9, D3Q15, D3Q19, D3Q27, Stencil, TorchStencil
 from ._unit import UnitConversion
 from ._flow import (Boundary, Equilibrium, Flow, QuadraticEquilibrium,
+                    QuadraticEquilibriumLessMemory,
                     initialize_f_neq, torch_gradient)
 from ._collision import (BGKCollision, Collision, KBCCollision, MRTCollision, NoCollision,
                          RegularizedCollision, SmagorinskyCollision, TRTCollision)
@@ -37,7 +38,8 @@ __version__ = "0.1.0"
 
 __all__ = [
     "Context", "Stencil", "TorchStencil", "D1Q3", "D2Q9", "D3Q15", "D3Q19", "D3Q27",
-    "UnitConversion", "Flow", "Equilibrium", "QuadraticEquilibrium", "Boundary",
+    "UnitConversion", "Flow", "Equilibrium", "QuadraticEquilibrium",
+    "QuadraticEquilibriumLessMemory", "Boundary",
     "initialize_f_neq", "torch_gradient", "Collision", "BGKCollision",
     "TRTCollision", "KBCCollision", "NoCollision", "BounceBackBoundary",
     "EquilibriumBoundaryPU", "AntiBounceBackOutlet", "EquilibriumOutletP",

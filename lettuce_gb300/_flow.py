@@ -21,7 +21,7 @@ from . import _device, _lib
 from ._native import NativeQuadraticEquilibrium
 from ._stencil import TorchStencil
 
-__all__ = ["Equilibrium", "QuadraticEquilibrium", "Boundary", "Flow",
+__all__ = ["Equilibrium", "QuadraticEquilibrium", "QuadraticEquilibriumLessMemory", "Boundary", "Flow",
            "torch_gradient", "initialize_f_neq"]
 
 
@@ -60,6 +60,13 @@ class QuadraticEquilibrium(Equilibrium):
 
     def native_generator(self):
         return NativeQuadraticEquilibrium()
+
+
+class QuadraticEquilibriumLessMemory(QuadraticEquilibrium):
+    """lettuce's lower-memory form of the same quadratic equilibrium
+    (lettuce/ext/_equilibrium/quadratic_equilibrium_less_memory.py:8-30,
+    "does the same as the normal equilibrium"): here the same torch
+    expression and the same step kernels."""
 
 
 class Boundary(ABC):

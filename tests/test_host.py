@@ -237,3 +237,15 @@ def test_checkpoint_compatible_with_lettuce(tmp_path):
     with open(tmp_path / "ours.pkl", "rb") as fh:
         back = pickle.load(fh)
     assert isinstance(back, np.ndarray) and np.array_equal(back, ref)
+
+
+def test_lower_memory_equilibrium_is_the_quadratic_one():
+    """lettuce's QuadraticEquilibriumLessMemory evaluates the same
+    equilibrium; here it is accepted by the step (same kernels)"""
+    import lettuce_gb300 as lt
+    ctx = lt.Context("cpu", torch.float64)
+    eq = lt.QuadraticEquilibriumLessMemory()
+    flow = lt.TaylorGreenVortex(ctx, [8, 6], 100, 0.05, lt.D2Q9, equilibrium=eq)
+    assert torch.equal(eq(flow), lt.QuadraticEquilibrium()(flow))
+    assert eq.native_available()
+    lt.Simulation(flow, lt.BGKCollision(0.7), [])   # set-up accepts it
