@@ -337,3 +337,47 @@ def test_drag_and_lift_coefficients(lgb):
     sim.reporter.append(rep)
     sim(2)
     assert len(rep.out) >= 1 and np.isfinite(np.asarray(rep.out[-1][-1], dtype=float)).all()
+
+
+@pytest.mark.parametrize("kind", ["halfway", "interpolated"])
+def test_momentum_balance_periodic_box(lgb, kind):
+    """periodic D3Q19 Taylor-Green 64^3 around a sphere, float64 BGK: the
+    collision conserves momentum and the solid cells keep theirs, so over n
+    steps the total momentum changes by minus the sum of the boundary's
+    momentum-exchange forces"""
+    from lgb_helpers import HwbbFlow
+    res = [64, 64, 64]
+    ctx = lt.Context("cuda:0", torch.float64)
+    tgv = lt.TaylorGreenVortex(ctx, res, 400, 0.05, lt.D3Q19)
+    f0 = tgv.f.cpu().numpy()
+    st = lt.D3Q19()
+    g = np.meshgrid(*[np.arange(k) for k in res], indexing="ij", sparse=True)
+    centre = [30.3, 33.1, 31.7]
+    solid = sum((gi - ci) ** 2 for gi, ci in zip(g, centre)) < 8.0 ** 2
+    flow = HwbbFlow(ctx, st, f0)
+    sbd = lt.SolidBoundaryData()
+    sbd.solid_mask = solid
+    if kind == "halfway":
+        b = lt.HalfwayBounceBackBoundary(ctx, flow, sbd, periodicity=(True, True, True),
+                                         calc_force=True)
+    else:
+        rows = lt.hwbb_links(st.e, st.opposite, solid, None, (True, True, True))
+        d = np.random.default_rng(2).uniform(0.05, 0.95, len(rows))
+        small = d < 0.5
+        sbd.f_index_lt, sbd.f_index_gt = rows[small], rows[~small]
+        sbd.d_lt, sbd.d_gt = d[small], d[~small]
+        b = lt.LinearInterpolatedBounceBackBoundary(ctx, flow, sbd, calc_force=True)
+    flow.psb = [b]
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.62), [])
+
+    def total_momentum():
+        return flow.j().sum(dim=(1, 2, 3)).cpu().numpy()
+
+    j0 = total_momentum()
+    fsum = np.zeros(3)
+    for _ in range(20):
+        sim(1)
+        fsum += to_np(b.force_sum)
+    dj = total_momentum() - j0
+    assert np.linalg.norm(fsum) > 1e-6
+    np.testing.assert_allclose(dj, -fsum, rtol=0, atol=1e-9 * np.abs(fsum).max() + 1e-12)
