@@ -282,3 +282,77 @@ def test_link_searches_equal_the_loops(stencil, shape):
         assert np.array_equal(lt.fwbb_links(st.e, st.opposite, mask, glob, per), want)
         want = _loop_search(st.e, st.opposite, mask, np.zeros_like(mask), per, at_solid=True)
         assert np.array_equal(lt.fwbb_links(st.e, st.opposite, mask, None, per), want)
+
+
+def test_ebb_masks_with_ordinary_boundaries_on_cpu(oracle):
+    """an equilibrium inlet and an anti-bounce-back outlet (lettuce's
+    post-collision boundaries) plus a halfway, an interpolated and a
+    full-way solid: the masks EbbSimulation builds equal the oracle's
+    restatement of ebb_simulation.py:28-57"""
+    from lgb_helpers import HwbbFlow
+    res = [18, 9]
+    st = lt.D2Q9()
+    rng = np.random.default_rng(4)
+    f0 = np.asarray(st.w).reshape(-1, 1, 1) * (1 + 0.01 * rng.standard_normal([9] + res))
+    ctx = lt.Context("cpu", torch.float64)
+    flow = HwbbFlow(ctx, st, f0)
+    inlet = np.zeros(res, dtype=bool)
+    inlet[0] = True
+    flow._bnds = [lt.EquilibriumBoundaryPU(ctx, flow, torch.as_tensor(inlet),
+                                           torch.tensor([0.01, 0.0], dtype=torch.float64)),
+                  lt.AntiBounceBackOutlet([1, 0], flow)]
+    s1 = np.zeros(res, dtype=bool)
+    s1[3:5, 2:5] = True
+    s2 = np.zeros(res, dtype=bool)
+    s2[8:10, 4:7] = True
+    s3 = np.zeros(res, dtype=bool)
+    s3[13:15, 1:3] = True
+    glob = s1 | s2 | s3
+    d1 = lt.SolidBoundaryData()
+    d1.solid_mask = s1
+    hw = lt.HalfwayBounceBackBoundary(ctx, flow, d1, global_solid_mask=glob)
+    rows = lt.hwbb_links(st.e, st.opposite, s2, glob)
+    d2 = lt.SolidBoundaryData()
+    d2.solid_mask = s2
+    d2.f_index_lt, d2.f_index_gt = rows[:5], rows[5:]
+    d2.d_lt, d2.d_gt = np.full(5, 0.3), np.full(len(rows) - 5, 0.7)
+    ib = lt.LinearInterpolatedBounceBackBoundary(ctx, flow, d2)
+    fw = lt.FullwayBounceBackBoundary(ctx, flow, s3, global_solid_mask=glob, calc_force=True)
+    flow.psb = [hw, ib, fw]
+    sim = lt.EbbSimulation(flow, lt.BGKCollision(0.7), [])
+    post = [{"kind": "equilibrium_pu", "mask": inlet, "rho": np.ones([1, 1]),
+             "u": np.zeros([2, 1, 1])},
+            {"kind": "anti_bounce_back", "direction": [1, 0]}]
+    ps = [dict(solid=s1, f_index=hw.f_index.numpy()),
+          dict(solid=s2, f_index=rows, d=np.r_[np.full(5, 0.3), np.full(len(rows) - 5, 0.7)]),
+          dict(solid=s3, f_index=fw.f_index_fwbb.numpy(), fullway=True)]
+    ncm, nsm = oracle.ebb_masks(res, 9, "D2Q9", [], post, ps)
+    assert np.array_equal(sim.no_collision_mask.numpy(), ncm)
+    assert np.array_equal(sim.no_streaming_mask.numpy(), nsm)
+    assert set(np.unique(ncm)) == {0, 1, 2, 3, 4, 5}
+    # every link in the table once; the force triplets are the full-way ones
+    assert sim._desc.n_links == len(hw.f_index) + len(rows) + len(fw.f_index_fwbb)
+    trip = sim._force_links.numpy().view(np.uint32)
+    assert len(trip) == len(fw.f_index_fwbb) and np.all(trip[:, 2] & 0x80000000)
+
+
+def test_bench_sphere_distances():
+    """the bench's wall distances put x + d e_q on the sphere's surface"""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "bench_mod", os.path.join(os.path.dirname(os.path.dirname(__file__)), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    res = [40, 20, 20]
+    centre, r = [12.0, 9.5, 9.5], 4.3
+    g = np.meshgrid(*[np.arange(k) for k in res], indexing="ij", sparse=True)
+    solid = sum((gi - ci) ** 2 for gi, ci in zip(g, centre)) < r * r
+    st = lt.D3Q27()
+    rows = lt.hwbb_links(st.e, st.opposite, solid)
+    d = bench.sphere_link_distances(rows, centre, r)
+    e = np.asarray(st.e)[rows[:, 0]]
+    p = rows[:, 1:] + d[:, None] * e
+    dist = np.sqrt(np.sum((p - np.asarray(centre)) ** 2, axis=1))
+    assert np.all((d > 0) & (d <= 1))
+    np.testing.assert_allclose(dist[d > 1e-3], r, rtol=1e-9)
