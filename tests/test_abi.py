@@ -159,3 +159,26 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "library_path", lambda: str(tmp_path / "nope.so"))
     with pytest.raises(_lib.LibraryError, match="no fallback"):
         _lib.load()
+
+
+def test_batch_struct_layouts_match_header(tmp_path, lgb):
+    """the numpy / ctypes mirrors of the batch tables and descriptor have
+    the header's sizes and offsets"""
+    from lettuce_gb300._batched import DOMAIN_DTYPE, TILE_DTYPE, BatchDesc
+    src = tmp_path / "probe_batch.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "lettuce_gb300.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu\\n\","
+        " sizeof(lgb_batch_domain), offsetof(lgb_batch_domain, tau),"
+        " sizeof(lgb_batch_tile), sizeof(lgb_batch_desc),"
+        " offsetof(lgb_batch_desc, domains), offsetof(lgb_batch_desc, f_out),"
+        " offsetof(lgb_batch_desc, pool_elements), offsetof(lgb_batch_desc, status));"
+        "return 0;}\n")
+    exe = tmp_path / "probe_batch"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == [DOMAIN_DTYPE.itemsize, DOMAIN_DTYPE.fields["tau"][1], TILE_DTYPE.itemsize,
+                   ctypes.sizeof(BatchDesc), BatchDesc.domains.offset, BatchDesc.f_out.offset,
+                   BatchDesc.pool_elements.offset, BatchDesc.status.offset]
