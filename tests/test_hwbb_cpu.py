@@ -356,3 +356,43 @@ def test_bench_sphere_distances():
     dist = np.sqrt(np.sum((p - np.asarray(centre)) ** 2, axis=1))
     assert np.all((d > 0) & (d <= 1))
     np.testing.assert_allclose(dist[d > 1e-3], r, rtol=1e-9)
+
+
+def test_boundaries_without_links_on_cpu():
+    """an empty solid and a solid enclosed by other solids give no links:
+    the descriptors still describe a valid launch (no value table, a force
+    over zero links)"""
+    from lgb_helpers import HwbbFlow
+    res = [8, 6]
+    st = lt.D2Q9()
+    f0 = np.asarray(st.w).reshape(-1, 1, 1) * np.ones([9] + res)
+    ctx = lt.Context("cpu", torch.float64)
+    empty = np.zeros(res, dtype=bool)
+    inner = np.zeros(res, dtype=bool)
+    inner[3, 2] = True
+    ring = np.zeros(res, dtype=bool)
+    ring[2:5, 1:4] = True
+    ring[3, 2] = False
+    for kind in ("halfway", "interpolated", "fullway"):
+        for solid, glob in ((empty, None), (inner, inner | ring)):
+            flow = HwbbFlow(ctx, st, f0)
+            sbd = lt.SolidBoundaryData()
+            sbd.solid_mask = solid
+            if kind == "halfway":
+                b = lt.HalfwayBounceBackBoundary(ctx, flow, sbd, global_solid_mask=glob,
+                                                 calc_force=True)
+            elif kind == "interpolated":
+                sbd.f_index_lt = np.zeros((0, 3), dtype=np.int64)
+                sbd.f_index_gt = np.zeros((0, 3), dtype=np.int64)
+                sbd.d_lt, sbd.d_gt = np.zeros(0), np.zeros(0)
+                b = lt.LinearInterpolatedBounceBackBoundary(ctx, flow, sbd, calc_force=True)
+            else:
+                b = lt.FullwayBounceBackBoundary(ctx, flow, solid, global_solid_mask=glob,
+                                                 calc_force=True)
+            assert len(b.link_rows()[0]) == 0
+            flow.psb = [b]
+            sim = lt.EbbSimulation(flow, lt.BGKCollision(0.7), [])
+            d = sim._desc
+            assert d.n_links == 0 and not d.link_val
+            assert d.n_force_links == 0 and d.force_out and d.force_scratch
+            assert int(sim._link_bits.abs().sum()) == 0
