@@ -6,6 +6,12 @@ Run in a container where the lettuce sources are available:
     PYTHONPATH=tests/golden/_stubs:/root/reference \
         python tests/golden/make_golden.py
 
+Options: ``--no-energy`` skips the long 256^2 energy-decay series;
+``--only-hwbb``, ``--only-ibb`` and ``--only-fwbb`` write only the cases of
+the efficient-bounce-back example's halfway, interpolated or full-way
+boundary (their modules are imported from the example's directory, found
+next to the imported lettuce package).
+
 ``_stubs/`` holds empty stand-ins for lettuce's optional imports (mmh3,
 h5py, pyevtk, matplotlib) -- none of them is on the arithmetic path. The
 outputs (``*.npz`` next to this script) are what the CPU oracle and the CUDA
