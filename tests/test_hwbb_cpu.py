@@ -396,3 +396,29 @@ def test_boundaries_without_links_on_cpu():
             assert d.n_links == 0 and not d.link_val
             assert d.n_force_links == 0 and d.force_out and d.force_scratch
             assert int(sim._link_bits.abs().sum()) == 0
+
+
+@pytest.mark.parametrize("kind", ["halfway", "interpolated"])
+def test_oracle_momentum_balance(oracle, kind):
+    """in the oracle, as in the kernels: on a periodic box the total
+    momentum changes by minus the summed momentum-exchange forces"""
+    st = lt.D2Q9()
+    res = [40, 30]
+    rng = np.random.default_rng(9)
+    e = np.asarray(st.e, dtype=np.float64)
+    w = np.asarray(st.w).reshape(-1, 1, 1)
+    f0 = w * (1.0 + 0.05 * rng.standard_normal([9] + res))
+    g = np.meshgrid(np.arange(res[0]), np.arange(res[1]), indexing="ij")
+    solid = (g[0] - 17.2) ** 2 + (g[1] - 14.6) ** 2 < 5.1 ** 2
+    rows = lt.hwbb_links(st.e, st.opposite, solid, None, (True, True))
+    b = dict(solid=solid, f_index=rows)
+    if kind == "interpolated":
+        b["d"] = rng.uniform(0.05, 0.95, len(rows))
+    steps = 25
+    forces = np.zeros((steps, 3))
+    f = oracle.run("D2Q9", f0, steps, collision="bgk", tau=0.66, post_streaming=[b],
+                   forces=forces)
+    dj = np.einsum("qd,qxy->d", e, f) - np.einsum("qd,qxy->d", e, f0)
+    fsum = forces.sum(axis=0)[:2]
+    assert np.abs(fsum).max() > 1e-3
+    np.testing.assert_allclose(dj, -fsum, rtol=0, atol=1e-11)
