@@ -12,7 +12,7 @@
  *
  * Layout of a population field: lettuce's [Q, *resolution], C-contiguous,
  * the last lettuce dimension fastest (lettuce/_flow.py:92). The q ordering is
- * lettuce's (lettuce/ext/_stencil/*.py).
+ * lettuce's (the stencil modules in lettuce/ext/_stencil/).
  */
 #ifndef LETTUCE_GB300_H
 #define LETTUCE_GB300_H
