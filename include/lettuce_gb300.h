@@ -245,12 +245,16 @@ int lgb_reduce(int32_t stencil, int32_t storage, const int32_t *res,
  * Scratch: a file-scope device array of LGB_REDUCE_STATIC_SCRATCH_BYTES
  * (48,640 bytes), held by every GPU that loads this library until the
  * process exits. The reduction's scratch need does not grow with the field
- * (a fixed grid of partial sums), so every grid the library accepts fits; a
- * need above the array size is rejected with an error. The call allocates
- * nothing (no cudaMalloc, no allocating library routine).
+ * (a fixed grid of 1216 partial sums of 5 doubles, checked against the array
+ * size when the library is compiled), so every grid the library accepts
+ * fits. The call allocates nothing (no cudaMalloc, no allocating library
+ * routine).
  * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. All calls share the one array: calls that
+ * (cudaGetSymbolAddress) with that device current and keeps it for the
+ * process; make that first call before any stream capture. The kept address
+ * belongs to the device's context of that time: after cudaDeviceReset on a
+ * device, do not call lgb_reduce_static on it again in this process (reload
+ * is not supported). All calls share the one array: calls that
  * overlap on the GPU (different streams, no ordering between them) race and
  * corrupt each other's results -- order them (same stream or events). The
  * array keeps the last call's partial sums; each call writes every partial

@@ -1,7 +1,8 @@
 """Device, dtype and population storage of a simulation.
 
-Mirrors lettuce's ``Context`` (lettuce/_context.py:9-122): same constructor
-arguments, same validation and tensor factories. One addition: ``storage``
+Mirrors lettuce's ``Context`` (lettuce/_context.py:9-122): the same
+constructor arguments and tensor factories, and the same placements (a
+contradictory device / use_native pair raises AssertionError, as in lettuce). One addition: ``storage``
 selects the population storage format of the GB300 kernels:
 
 * ``None`` -- the population field is stored in ``dtype`` (float32/float64);
@@ -31,56 +32,80 @@ _STORAGE = {
 }
 
 
+def _need(ok: bool, message: str):
+    """lettuce signals a contradictory context with AssertionError; raise
+    the same type (explicitly, so that ``python -O`` keeps the check)"""
+    if not ok:
+        raise AssertionError(message)
+
+
+def _placement(device, use_native):
+    """(torch.device, use_native) for the constructor's arguments.
+
+    ============  ==========  =========================================
+    device        use_native  result
+    ============  ==========  =========================================
+    None          None        cuda:0 and native if torch sees a GPU,
+                              else cpu without native
+    None          True/False  cuda:0; True needs a visible GPU
+    cuda[:k]      any         needs a visible GPU; native unless False
+    cpu           None/False  cpu, not native
+    cpu           True        refused
+    other         any         refused
+    ============  ==========  =========================================
+    """
+    gpu = torch.cuda.is_available()
+    if device is None:
+        if use_native is None:
+            return torch.device("cuda:0" if gpu else "cpu"), gpu
+        _need(gpu or not use_native,
+              "use_native=True asks for the GPU kernels, but torch sees no CUDA device")
+        return torch.device("cuda:0"), bool(use_native)
+    kind = str(device)
+    if "cuda" in kind:
+        _need(gpu, f"device {kind!r} was requested, but torch sees no CUDA device")
+        return torch.device(device), True if use_native is None else bool(use_native)
+    _need("cpu" in kind, f"device {kind!r}: lettuce_gb300 places flows on 'cpu' (set-up "
+                         "only) or on a 'cuda' device")
+    _need(not use_native, "use_native=True runs the GPU kernels and cannot be combined "
+                          "with a cpu device")
+    return torch.device(device), False
+
+
+def _is_mask_dtype(array) -> bool:
+    """boolean and uint8 arrays / tensors keep an integer type when they are
+    converted (lettuce turns masks into uint8, not into the float dtype)"""
+    dt = getattr(array, "dtype", None)
+    if dt is None:
+        return False
+    if isinstance(dt, torch.dtype):
+        return dt in (torch.bool, torch.uint8)
+    try:
+        return np.dtype(dt) in (np.dtype(np.bool_), np.dtype(np.uint8))
+    except TypeError:
+        return False
+
+
 class Context:
     def __init__(self, device: Optional[Union[torch.device, str]] = None,
                  dtype: Optional[torch.dtype] = None,
                  use_native: Optional[bool] = None,
                  storage: Optional[str] = None):
-        if device is None and use_native is None:
-            device = torch.device("cuda:0" if torch.cuda.is_available() else "cpu")
-            use_native = torch.cuda.is_available()
-        elif device is None:
-            assert not use_native or torch.cuda.is_available(), \
-                "native CUDA path requested but CUDA is not available!"
-            device = torch.device("cuda:0")
-        elif use_native is None:
-            if "cuda" in str(device):
-                assert torch.cuda.is_available(), \
-                    "cuda device explicitly requested but cuda is not available!"
-                use_native = True
-            else:
-                assert "cpu" in str(device), \
-                    f"lettuce_gb300 works on cpu (set-up) or cuda devices, not {device}"
-                use_native = False
-        else:
-            if "cuda" in str(device):
-                assert torch.cuda.is_available(), \
-                    "cuda device explicitly requested but cuda is not available!"
-            else:
-                assert "cpu" in str(device), \
-                    f"lettuce_gb300 works on cpu (set-up) or cuda devices, not {device}"
-                assert not use_native, \
-                    "can not use the native CUDA path on an explicitly requested cpu device!"
-
+        self.device, self.use_native = _placement(device, use_native)
         dtype = dtype or torch.float32
-        assert dtype in [torch.float16, torch.bfloat16, torch.float32, torch.float64], \
-            f"unsupported dtype {dtype}"
+        _need(dtype in (torch.float16, torch.bfloat16, torch.float32, torch.float64),
+              f"populations are float16, bfloat16, float32 or float64, not {dtype}")
         if storage not in _STORAGE:
             raise ValueError(f"unknown population storage {storage!r}; "
                              f"choose one of {[k for k in _STORAGE if k]}")
-        if dtype == torch.float16:
-            storage = storage or "fp16_shifted"
-        if dtype == torch.bfloat16:
-            storage = storage or "bf16_shifted"
-
-        self.device = torch.device(device)
-        self.use_native = bool(use_native)
+        # a 16-bit dtype means 16-bit storage with float32 arithmetic
+        storage = storage or {torch.float16: "fp16_shifted",
+                              torch.bfloat16: "bf16_shifted"}.get(dtype)
         self.storage_name = storage
         if storage is None:
             self.dtype = dtype
             self.storage = _lib.F64 if dtype == torch.float64 else _lib.F32
         else:
-            # compute (and moment) type of the 16-bit formats is float32
             self.dtype = torch.float32
             self.storage = _STORAGE[storage]
 
@@ -117,18 +142,13 @@ class Context:
 
     def convert_to_tensor(self, array, *args, dtype: Optional[torch.dtype] = None,
                           **kwargs) -> torch.Tensor:
-        new_dtype = dtype
-        if dtype is None:
-            bool_types = [bool, torch.bool, torch.uint8, np.uint8]
-            if hasattr(array, "dtype") and array.dtype in bool_types:
-                new_dtype = torch.uint8
-            else:
-                new_dtype = self.dtype
-        if isinstance(array, torch.Tensor):
-            return array.to(*args, **kwargs, device=self.device, dtype=new_dtype)
-        array = np.ascontiguousarray(np.array(array))
-        return torch.from_numpy(array).to(*args, **kwargs, device=self.device,
-                                          dtype=new_dtype)
+        """``array`` (tensor, ndarray, list or number) on this context's
+        device; in ``dtype`` if given, else uint8 for boolean / uint8 input
+        and the context dtype for everything else"""
+        target = dtype or (torch.uint8 if _is_mask_dtype(array) else self.dtype)
+        if not isinstance(array, torch.Tensor):
+            array = torch.from_numpy(np.ascontiguousarray(np.asarray(array)))
+        return array.to(*args, **kwargs, device=self.device, dtype=target)
 
     @staticmethod
     def convert_to_ndarray(tensor) -> np.ndarray:

@@ -878,6 +878,12 @@ int lgb_reduce(int32_t stencil, int32_t storage, const int32_t *res, const void 
 
 static __device__ __align__(256) double g_reduce_scratch[LGB_REDUCE_STATIC_SCRATCH_BYTES / sizeof(double)];
 
+// the reduction launches a fixed grid of kReduceBlocks blocks whatever the
+// field size, so its scratch need is a build-time constant
+static_assert((int64_t)kReduceBlocks * LGB_REDUCE_FIELDS * (int64_t)sizeof(double) <=
+                  (int64_t)LGB_REDUCE_STATIC_SCRATCH_BYTES,
+              "the reduction's partial sums do not fit the static scratch array");
+
 namespace {
 
 constexpr int kMaxDevices = 64;
@@ -885,7 +891,10 @@ std::mutex g_scratch_mutex;
 void *g_scratch_addr[kMaxDevices] = {};
 
 // device address of g_reduce_scratch on the current device, looked up once
-// per device (the host-side name g_reduce_scratch is not a device address)
+// per device (the host-side name g_reduce_scratch is not a device address).
+// The cached address belongs to the device's context at the time of the
+// lookup: after cudaDeviceReset the process must not call
+// lgb_reduce_static on that device again (the header says so)
 int static_scratch_address(void **ptr) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -914,8 +923,9 @@ int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res, cons
     if (make_grid(stencil, res, &g)) return -1;
     if (!valid_storage(storage)) return fail("lgb_reduce_static: unknown storage id %d", storage);
     if (!f || !out) return fail("lgb_reduce_static: NULL pointer");
-    // the partial sums this reduction writes; it launches a fixed grid of
-    // kReduceBlocks blocks whatever the field size
+    // the partial sums this call writes (a fixed grid of kReduceBlocks
+    // blocks whatever the field size; the static_assert above holds it to
+    // the array at build time, this keeps the run-time refusal beside it)
     const int64_t need = lgb_reduce_scratch_bytes();
     if (need > (int64_t)LGB_REDUCE_STATIC_SCRATCH_BYTES)
         return fail("lgb_reduce_static: the reduction needs %lld bytes of scratch, the static "

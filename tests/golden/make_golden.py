@@ -3,7 +3,7 @@
 Run in a container where the lettuce sources are available:
 
     PYTHONDONTWRITEBYTECODE=1 \
-    PYTHONPATH=tests/golden/_stubs:/root/reference \
+    PYTHONPATH=tests/golden/_stubs:<lettuce checkout> \
         python tests/golden/make_golden.py
 
 Options: ``--no-energy`` skips the long 256^2 energy-decay series;

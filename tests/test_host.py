@@ -159,6 +159,22 @@ def test_context_semantics():
         lt.Context("cpu", use_native=True)
     with pytest.raises(ValueError):
         lt.Context("cpu", storage="fp8")
+    with pytest.raises(AssertionError):
+        lt.Context("mps")
+    if not torch.cuda.is_available():
+        with pytest.raises(AssertionError):
+            lt.Context("cuda:0")
+        with pytest.raises(AssertionError):
+            lt.Context(None, use_native=True)
+        # lettuce's placement without a device but with use_native=False
+        assert lt.Context(None, use_native=False).device == torch.device("cuda:0")
+        assert lt.Context().device == torch.device("cpu") and not lt.Context().use_native
+    # masks keep an integer type, everything else takes the context dtype
+    assert c.convert_to_tensor(np.array([True, False])).dtype == torch.uint8
+    assert c.convert_to_tensor(torch.zeros(2, dtype=torch.bool)).dtype == torch.uint8
+    assert c.convert_to_tensor([1, 2]).dtype == torch.float32
+    assert c.convert_to_tensor(0.1).item() == np.float32(0.1)
+    assert lt.Context("cpu", torch.float64).convert_to_tensor(np.arange(3)).dtype == torch.float64
 
 
 def test_shifted_storage_round_trip_on_host():
