@@ -5,10 +5,13 @@ Workload (one "step" = one LBM time step over the whole grid): D3Q19 BGK
 one pull-pattern pass (lettuce PRE_STREAMING, the CLI benchmark default).
 Populations stored as float32 (headline ``value``) and as shifted float16
 with float32 arithmetic (``fp16_shifted``); the in-place AA variants are
-reported beside them. The 16-bit run's velocity error against a float64 run
-of the same 1000 steps is measured in ``accuracy``. ``configs`` holds short
-timed runs of the other configurations of the family (D3Q27 KBC obstacle,
-256 batched D2Q9 domains, the D2Q9 adjoint); ``--no-configs`` skips them.
+reported beside them. ``accuracy`` holds the 16-bit runs' velocity error
+after 1000 steps against the float64 oracle (summarised in
+tests/golden/accuracy_pin_d3q19_256_f64_1000.npz, matched by the float64
+kernels). ``configs`` holds timed runs of the other configurations of the
+family (D3Q27 KBC obstacle, also over its full 5000 steps with the sphere's
+drag, 256 batched D2Q9 domains, the D2Q9 adjoint); ``--no-configs`` skips
+them.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -254,26 +257,75 @@ def time_variant(lt, torch, storage, pattern, steps, warmup, device):
     return ms, flow, sim
 
 
-def accuracy_fp16(lt, torch, device, steps=1000):
-    """relative L2 velocity error of fp16-shifted (and bf16) storage after
-    ``steps`` steps against a float64 run of the same workload"""
+PIN = os.path.join(ROOT, "tests", "golden", "accuracy_pin_d3q19_256_f64_1000.npz")
+
+
+def accuracy_vs_oracle(lt, torch, device, steps=1000):
+    """relative L2 velocity error of the shifted 16-bit storages (and of
+    float32) after ``steps`` steps against the float64 reference of the same
+    workload. The reference is the float64 C oracle (lettuce's step restated,
+    pinned to lettuce-generated vectors): its 256^3 x 1000-step field is
+    summarised in tests/golden/accuracy_pin_d3q19_256_f64_1000.npz (u at 8192
+    cells, plane sums over every cell, totals). The float64 kernels run the same
+    steps here; their field must match those summaries, and the errors are
+    taken over the whole field against it, and over the 8192 cells against
+    the oracle's own values."""
+    pre = lt.StreamingStrategy.PRE_STREAMING
     ref = lt.TaylorGreenVortex(lt.Context(device, torch.float64), RES, RE, MA, lt.D3Q19)
     tau = ref.units.relaxation_parameter_lu
-    pre = lt.StreamingStrategy.PRE_STREAMING
     lt.Simulation(ref, lt.BGKCollision(tau), [], pre)(steps)
     u_ref = ref.u()
     del ref
     torch.cuda.empty_cache()
-    out = {}
-    for storage in ["fp16_shifted", None]:
+    out = {"steps": steps}
+    pin = None
+    if steps == 1000 and RES == [256, 256, 256] and os.path.exists(PIN):
+        pin = np.load(PIN)
+        cells = torch.as_tensor(pin["cells"], device=device)
+        u_s = torch.as_tensor(pin["u_samples"], device=device)
+        flat = u_ref.reshape(3, -1)
+        got = flat[:, cells]
+        umax = float(torch.max(torch.abs(u_s)))
+        def plane_sums(a):
+            return torch.stack([a.sum(dim=(1, 2)), a.sum(dim=(0, 2)), a.sum(dim=(0, 1))])
+        ups = torch.stack([plane_sums(u_ref[c] * u_ref[c]) for c in range(3)])
+        ups_ref = torch.as_tensor(pin["u_sq_plane_sums"], device=device)
+        usq = torch.stack([torch.sum(u_ref[c] * u_ref[c]) for c in range(3)]).cpu().numpy()
+        out["reference"] = ("float64 C oracle (lettuce's torch step restated, pinned to "
+                            "lettuce-generated vectors): 256^3 x 1000 steps summarised in "
+                            "tests/golden/accuracy_pin_d3q19_256_f64_1000.npz; errors over "
+                            "the full field against the float64 kernels' field, which "
+                            "matches it as f64_kernel_vs_oracle shows")
+        out["f64_kernel_vs_oracle"] = {
+            "max_abs_u_at_samples_over_max_u": float(torch.max(torch.abs(got - u_s))) / umax,
+            "max_rel_plane_sum_u_sq": float(torch.max(
+                torch.abs(ups - ups_ref) / torch.amax(torch.abs(ups_ref), dim=2, keepdim=True))),
+            "rel_sum_u_sq": float(np.max(np.abs(usq / pin["u_sq_sums"] - 1))),
+            "samples": int(len(pin["cells"]))}
+    else:
+        out["reference"] = "float64 run of the same kernels (no oracle summary for this size)"
+    errs, errs_s = {}, {}
+    for storage in ["fp16_shifted", "bf16_shifted", None]:
         low = lt.TaylorGreenVortex(lt.Context(device, torch.float32, storage=storage),
                                    RES, RE, MA, lt.D3Q19)
         lt.Simulation(low, lt.BGKCollision(tau), [], pre)(steps)
         u = low.u().to(torch.float64)
-        err = (torch.linalg.vector_norm(u - u_ref) / torch.linalg.vector_norm(u_ref)).item()
-        out[storage or "f32"] = err
-        del low
+        key = storage or "f32"
+        errs[key] = (torch.linalg.vector_norm(u - u_ref)
+                     / torch.linalg.vector_norm(u_ref)).item()
+        if pin is not None:
+            us = u.reshape(3, -1)[:, cells]
+            errs_s[key] = (torch.linalg.vector_norm(us - u_s)
+                           / torch.linalg.vector_norm(u_s)).item()
+        del low, u
         torch.cuda.empty_cache()
+    out["u_rel_l2"] = errs
+    if errs_s:
+        out["u_rel_l2_at_oracle_samples"] = errs_s
+    out["target"] = "fp16_shifted <= 1e-3 (north star); bf16_shifted misses it"
+    out["u_rel_l2_fp16_shifted"] = errs["fp16_shifted"]
+    out["u_rel_l2_bf16_shifted"] = errs["bf16_shifted"]
+    out["u_rel_l2_f32"] = errs["f32"]
     return out
 
 
@@ -391,6 +443,190 @@ def time_bounce_back_obstacle(lt, torch, device, peak, g, steps, warmup):
     return out
 
 
+def config3_long_run(lt, torch, device, peak, steps=5000):
+    """config 3 over its full 5000 steps: the D3Q27 KBC channel 512x128x128
+    (sphere of diameter 24 as lettuce's full-way bounce-back, equilibrium
+    inlet, anti-bounce-back outlet, Re 300, float32, PRE streaming) with its
+    status word (bit 0: a non-finite density) and the mass change; then the
+    same channel with the sphere as the example project's halfway
+    bounce-back computing the momentum exchange every step, its drag and
+    lift coefficients sampled every 100 steps over the last 1000 (the
+    example's F / (0.5 rho_mean u^2 pi r^2), r = 12)"""
+    import math
+    g = 256
+    res = [2 * g, g // 2, g // 2]
+    n = int(np.prod(res))
+    r = 12.0
+    centre = [g / 2, (res[1] - 1) / 2, (res[2] - 1) / 2]
+    grid = np.meshgrid(*[np.arange(k) for k in res], indexing="ij", sparse=True)
+    solid = sum((gi - ci) ** 2 for gi, ci in zip(grid, centre)) < r * r
+    out = {"workload": "D3Q27 KBC obstacle 512x128x128, float32, 5000 steps", "steps": steps}
+
+    flow = lt.Obstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                       res[0] / 24.0, stencil=lt.D3Q27)
+    flow.mask = solid
+    flow.initialize()
+    sim = lt.Simulation(flow, lt.KBCCollision(), [],
+                        streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+    from lettuce_gb300._reporter import reduce_flow
+    m0 = reduce_flow(flow)
+    stream = torch.cuda.current_stream(device)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    start.record(stream)
+    sim(steps)
+    end.record(stream)
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    m1 = reduce_flow(flow)
+    m0, m1 = m0.cpu().numpy(), m1.cpu().numpy()
+    umax = float(np.sqrt(m1[2]))
+    out["full_way_bounce_back"] = {
+        "status": sim.status, "nonfinite_cells": int(m1[3]),
+        "mass_rel_change": float(m1[0] / m0[0] - 1), "max_u_lu": round(umax, 5),
+        "ms_per_step": round(ms, 4), "mlups": round(n / (ms * 1e-3) / 1e6, 1),
+        "frac_of_peak": round(217 * n / (ms * 1e-3) / 1e9 / peak, 4)}
+    del sim, flow
+    torch.cuda.empty_cache()
+
+    class EbbObstacle(lt.Obstacle):
+        psb = ()
+
+        @property
+        def post_streaming_boundaries(self):
+            return list(self.psb)
+
+    flow = EbbObstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                       res[0] / 24.0, stencil=lt.D3Q27)
+    flow.initialize()
+    sbd = lt.SolidBoundaryData()
+    sbd.solid_mask = solid
+    b = lt.HalfwayBounceBackBoundary(flow.context, flow, sbd, calc_force=True)
+    flow.psb = [b]
+    sim = lt.EbbSimulation(flow, lt.KBCCollision(), [])
+    area_pu = math.pi * 0.5 ** 2  # the sphere's cross-section, diameter 1 in physical units
+    drag = lt.DragCoefficient(flow, b, solid, area_pu)
+    lift = lt.LiftCoefficient(flow, b, solid, area_pu)
+    sim(steps - 1000)
+    cd, cl = [], []
+    for _ in range(10):
+        sim(100)
+        cd.append(float(drag()))
+        cl.append(float(lift()))
+    out["halfway_bounce_back"] = {
+        "status": sim.status, "drag_coefficient": round(float(np.mean(cd)), 4),
+        "drag_coefficient_range": [round(min(cd), 4), round(max(cd), 4)],
+        "lift_coefficient": round(float(np.mean(cl)), 4),
+        "sampled": "every 100 steps over steps 4001-5000"}
+    del sim, flow, b, drag, lift
+    torch.cuda.empty_cache()
+    return out
+
+
+def config5_adjoint(lt, torch, device, nn=512, steps=200, k=20, reps=5):
+    """config 5: D2Q9 BGK 512^2 float32 (Re 1000, Ma 0.05), Taylor-Green
+    velocity plus a seeded 1e-3 N(0,1) perturbation, loss = MSE(u(200),
+    seeded target); gradient w.r.t. the initial velocity through the
+    hand-written adjoint with a checkpoint every 20 steps. CUDA events on the
+    current stream: the forward pass (equilibrium, 200 steps, moments,
+    loss) and loss.backward() (segment recompute and adjoint steps from
+    captured graphs), best of ``reps``; plus the per-step time of the
+    forward step and of the adjoint kernel alone, each replayed 200 times
+    from a graph of 20 launches. The field is 9.4 MB (float32) and stays in
+    the 129 MB L2, so HBM does not bound these launches: at a few
+    microseconds per kernel they are latency and launch bound."""
+    import ctypes
+    import math
+    ulu = 0.05 / math.sqrt(3)
+    x = torch.arange(nn, dtype=torch.float64) * 2 * math.pi / nn
+    XX, YY = torch.meshgrid(x, x, indexing="ij")
+    u0 = torch.stack([torch.cos(XX) * torch.sin(YY), -torch.sin(XX) * torch.cos(YY)]) * ulu
+    u0 = u0 + 1e-3 * torch.randn(u0.shape, generator=torch.Generator().manual_seed(0),
+                                 dtype=torch.float64)
+    target = ulu * torch.randn(u0.shape, generator=torch.Generator().manual_seed(1),
+                               dtype=torch.float64)
+    tau = 3 * ((nn / (2 * math.pi)) * ulu / 1000) + 0.5
+    u0 = u0.float().to(device)
+    target = target.float().to(device)
+    carrier = lt.TaylorGreenVortex(lt.Context(device, torch.float32), nn, 1000, 0.05, lt.D2Q9)
+    rho0 = torch.ones([1, nn, nn], dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+    fwd, bwd = [], []
+    for _ in range(reps):
+        u = u0.clone().requires_grad_(True)
+        e0, e1, e2 = ev(), ev(), ev()
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        f0 = lt.QuadraticEquilibrium()(carrier, rho0, u)
+        fT = lt.rollout(f0, carrier.stencil, tau, steps, checkpoint_every=k)
+        _, uT = lt.moments_torch(fT, carrier.stencil)
+        loss = torch.mean((uT - target) ** 2)
+        e1.record(stream)
+        loss.backward()
+        e2.record(stream)
+        torch.cuda.synchronize(device)
+        fwd.append(e0.elapsed_time(e1))
+        bwd.append(e1.elapsed_time(e2))
+    # single kernels, replayed from a graph of 20 launches
+    f = carrier.f_raw.contiguous()
+    g_ = torch.empty_like(f)
+    lam = torch.randn_like(f)
+    lam2 = torch.empty_like(f)
+    desc = lt._device.new_desc(lt._lib.D2Q9, lt._lib.F32, [nn, nn])
+    desc.collision = lt._lib.BGK
+    desc.tau = tau
+    desc.pattern = lt._lib.PULL
+    L = lt._lib.load()
+    r3 = lt._lib.i32x3([nn, nn])
+
+    def fwd20(st):
+        for i in range(20):
+            a, b = (f, g_) if i % 2 == 0 else (g_, f)
+            desc.f_in, desc.f_out = a.data_ptr(), b.data_ptr()
+            lt._device.step(desc, st)
+
+    def adj20(st):
+        for i in range(20):
+            a, b = (lam, lam2) if i % 2 == 0 else (lam2, lam)
+            lt._lib.check(L.lgb_adjoint_step(lt._lib.D2Q9, lt._lib.F32,
+                                             ctypes.cast(r3, ctypes.c_void_p), float(tau),
+                                             f.data_ptr(), a.data_ptr(), b.data_ptr(), st),
+                          "lgb_adjoint_step")
+    per = {}
+    for key, fn in (("forward_step_us", fwd20), ("adjoint_step_us", adj20)):
+        graph = lt._device.capture(device, fn)
+        graph.replay()
+        torch.cuda.synchronize(device)
+        a, b = ev(), ev()
+        a.record(stream)
+        for _ in range(10):
+            graph.replay()
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        per[key] = round(a.elapsed_time(b) * 1e3 / 200, 2)
+    f_ms, b_ms = min(fwd), min(bwd)
+    n_seg = steps // k
+    out = {"workload": "D2Q9 BGK 512^2 float32, 200 steps, checkpoint every 20",
+           "forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
+           "forward_mlups": round(steps * nn * nn / (f_ms * 1e-3) / 1e6, 1),
+           "forward_us_per_step": round(f_ms * 1e3 / steps, 2),
+           "backward_us_per_step": round(b_ms * 1e3 / steps, 2),
+           **per,
+           "backward_model_us": round(n_seg * ((k - 1) * per["forward_step_us"])
+                                      + steps * per["adjoint_step_us"], 1),
+           "bound": ("launch / latency: a 9.4 MB float32 field stays in the 129 MB L2; the "
+                     "backward pass runs k - 1 recomputed steps and k adjoint steps per "
+                     "segment (backward_model_us = segments x (k - 1) x forward step + "
+                     "steps x adjoint step)"),
+           "timing": "CUDA events on the current stream, best of %d" % reps}
+    del carrier, f, g_, lam, lam2
+    torch.cuda.empty_cache()
+    return out
+
+
 def measure_configs(lt, torch, device, peak):
     """the other configurations of the workload family, each at full size
     with a short timed run (CUDA events, inputs larger than L2):
@@ -412,6 +648,7 @@ def measure_configs(lt, torch, device, peak):
            "bytes_per_cell": 217}
     c3b.update(time_bounce_back_obstacle(lt, torch, device, peak, 256, 100, 10))
     out["config3_post_streaming_bounce_back"] = c3b
+    out["config3_5000_steps"] = config3_long_run(lt, torch, device, peak)
 
     c4 = {"workload": "256 D2Q9 TRT Taylor-Green domains, sides in [32, 512], Re in [100, 5000]"}
     for storage in (None, "fp16_shifted"):
@@ -440,42 +677,7 @@ def measure_configs(lt, torch, device, peak):
         torch.cuda.empty_cache()
     out["config4_batched"] = c4
 
-    nn = 512
-    ulu = 0.05 / math.sqrt(3)
-    x = torch.arange(nn, dtype=torch.float64) * 2 * math.pi / nn
-    XX, YY = torch.meshgrid(x, x, indexing="ij")
-    u0 = torch.stack([torch.cos(XX) * torch.sin(YY), -torch.sin(XX) * torch.cos(YY)]) * ulu
-    u0 = u0 + 1e-3 * torch.randn(u0.shape, generator=torch.Generator().manual_seed(0),
-                                 dtype=torch.float64)
-    target = ulu * torch.randn(u0.shape, generator=torch.Generator().manual_seed(1),
-                               dtype=torch.float64)
-    tau = 3 * ((nn / (2 * math.pi)) * ulu / 1000) + 0.5
-    u0 = u0.float().to(device)
-    target = target.float().to(device)
-    carrier = lt.TaylorGreenVortex(lt.Context(device, torch.float32), nn, 1000, 0.05, lt.D2Q9)
-    rho0 = torch.ones([1, nn, nn], dtype=torch.float32, device=device)
-    times = []
-    for _ in range(3):
-        u = u0.clone().requires_grad_(True)
-        torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        f0 = lt.QuadraticEquilibrium()(carrier, rho0, u)
-        fT = lt.rollout(f0, carrier.stencil, tau, 200, checkpoint_every=20)
-        _, uT = lt.moments_torch(fT, carrier.stencil)
-        loss = torch.mean((uT - target) ** 2)
-        torch.cuda.synchronize(device)
-        t1 = time.perf_counter()
-        loss.backward()
-        torch.cuda.synchronize(device)
-        times.append((t1 - t0, time.perf_counter() - t1))
-    fwd, bwd = min(t[0] for t in times), min(t[1] for t in times)
-    out["config5_adjoint"] = {
-        "workload": "D2Q9 BGK 512^2 float32, 200 steps, checkpoint every 20",
-        "forward_ms": round(fwd * 1e3, 2), "backward_ms": round(bwd * 1e3, 2),
-        "forward_mlups": round(200 * nn * nn / fwd / 1e6, 1),
-        "note": "host wall clock around synchronised calls, best of 3"}
-    del carrier
-    torch.cuda.empty_cache()
+    out["config5_adjoint"] = config5_adjoint(lt, torch, device)
     return out
 
 
@@ -563,12 +765,22 @@ def run_ours(args, world, rank, local):
     sim(args.warmup)
     torch.cuda.synchronize(device)
     barrier(world)
+    stream = torch.cuda.current_stream(device)
+    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     t0 = time.perf_counter()
+    ph[0].record(stream)
     flow.f = host
+    ph[1].record(stream)
     sim(args.steps)
+    ph[2].record(stream)
     flow.download(back)
+    ph[3].record(stream)
     torch.cuda.synchronize(device)
     e2e_s = allmax(time.perf_counter() - t0, world, device)
+    phases = {"h2d_ms": round(ph[0].elapsed_time(ph[1]), 3),
+              "steps_ms": round(ph[1].elapsed_time(ph[2]), 3),
+              "d2h_ms": round(ph[2].elapsed_time(ph[3]), 3),
+              "host_wall_ms": round(e2e_s * 1e3, 3)}
     e2e_mlups = args.steps * n_cells / e2e_s / 1e6 * world
     fbytes = host.numel() * host.element_size()
     del flow, sim, host, back
@@ -576,7 +788,7 @@ def run_ours(args, world, rank, local):
 
     acc = None
     if not args.no_accuracy:
-        acc = accuracy_fp16(lt, torch, device, steps=args.accuracy_steps)
+        acc = accuracy_vs_oracle(lt, torch, device, steps=args.accuracy_steps)
 
     configs = None
     if rank == 0 and not args.no_configs:
@@ -609,14 +821,13 @@ def run_ours(args, world, rank, local):
                          "frac_of_peak": f16["frac_of_peak"], "achieved_gbs": f16["achieved_gbs"],
                          "bytes_per_cell": BYTES_PER_CELL["f16"]},
         "variants": variants,
-        "accuracy": None if acc is None else {
-            "steps": args.accuracy_steps, "reference": "float64 run of the same kernels",
-            "u_rel_l2_fp16_shifted": acc.get("fp16_shifted"), "u_rel_l2_f32": acc.get("f32")},
+        "accuracy": acc,
         "e2e": {"value": round(e2e_mlups, 1), "unit": UNIT,
                 "h2d_bytes_per_step": int(fbytes / args.steps),
                 "d2h_bytes_per_step": int(fbytes / args.steps),
                 "call": f"flow.f = pinned host field; simulation({args.steps}); "
-                        "flow.download(pinned host field)"},
+                        "flow.download(pinned host field)",
+                "phases": phases},
         "cpu_baseline": cpu,
         "configs": configs,
         "clocks": clocks,

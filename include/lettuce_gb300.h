@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LGB_ABI_VERSION 3
+#define LGB_ABI_VERSION 4
 #define LGB_MAX_SUBSTEPS 8
 
 /* stencils (lettuce/ext/_stencil/d1q3.py, d2q9.py, d3q15.py, d3q19.py, d3q27.py) */
@@ -265,6 +265,42 @@ int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res,
                       const int32_t *hi, const uint8_t *mask, double *out,
                       void *stream);
 
+/* ---- initial fields and the enstrophy observable ------------------------ */
+
+/* Quadratic equilibrium populations of given density and velocity fields
+ * (lattice units, in the compute type: double for LGB_F64 storage, float
+ * otherwise), broadcast by element strides per lettuce dimension (0 =
+ * broadcast; u_stride[0] is the component stride), written into f ([Q][N]
+ * in `storage`) when f is not NULL. With rho_out / u_out (both or neither)
+ * the density [N] and velocity [D][N] of that equilibrium -- the moments
+ * lettuce reads back from the field it has just set -- are written as well;
+ * f may then be NULL. Replaces the initial equilibrium of
+ * lettuce/_flow.py:127-143 (Flow.initialize), evaluated in the order of
+ * lettuce/ext/_equilibrium/quadratic_equilibrium.py:11-24. */
+int lgb_equilibrium(int32_t stencil, int32_t storage, const int32_t *res, const void *rho,
+                    const int64_t *rho_stride, const void *u, const int64_t *u_stride,
+                    void *f, void *rho_out, void *u_out, void *stream);
+
+/* f = feq(rho, u) - fneq with the first-order non-equilibrium part
+ * fneq_q = w_q tau rho (d_b u_a) (e_qa e_qb - cs^2 delta_ab) / cs^2, the
+ * velocity gradient by 6th-order periodic central differences; rho [N] and
+ * u [D][N] contiguous in the compute type, D = 2 or 3. Replaces
+ * lettuce/_flow.py:341-367 (initialize_f_neq) with the differences of
+ * lettuce/util/utility.py:37-99 (torch_gradient, order 6). */
+int lgb_init_fneq(int32_t stencil, int32_t storage, const int32_t *res, const void *rho,
+                  const void *u, double tau, void *f, void *stream);
+
+/* out[0] = sum over cells of |curl u|^2 (2-D: (d_1 u_0 - d_0 u_1)^2; 3-D the
+ * three components), u [dims][N] contiguous in float64 (precision LGB_F64)
+ * or float32 (LGB_F32), lattice units, derivatives by 6th-order periodic
+ * central differences with dx = 1, accumulated in float64 through a fixed
+ * grid of partial sums folded in a fixed order. `scratch`: device memory of
+ * lgb_reduce_scratch_bytes() bytes. Enstrophy in physical units is
+ * out[0] * (u_pu / u_lu)^2 * dx^(dims - 2). Replaces
+ * lettuce/ext/_reporter/observable_reporter.py:45-67 (Enstrophy). */
+int lgb_enstrophy(int32_t dims, int32_t precision, const int32_t *res, const void *u,
+                  double *out, void *scratch, void *stream);
+
 /* ---- batched domains ---------------------------------------------------
  * Many periodic domains of different sizes, all with the same stencil,
  * storage and collision kind, advanced by one launch (the batched Taylor-
@@ -272,9 +308,14 @@ int lgb_reduce_static(int32_t stencil, int32_t storage, const int32_t *res,
  * counterpart). Domain b's populations are [Q][N_b] at element `offset` of
  * one pool; its relaxation times are per domain. */
 typedef struct {
-    int64_t offset;     /* element offset of the domain's [Q][N_b] field in the pool */
+    int64_t offset;     /* element offset of the domain's [Q][rows * pitch] field in the pool */
     int32_t res[3];     /* lettuce resolution; unused trailing dims = 1 */
-    int32_t reserved;
+    int32_t pitch;      /* elements from one row (last lettuce dimension) to the next;
+                           0 = the row length. The 16-bit shifted formats accept an odd
+                           row length stored with pitch = length + 1 (every row padded
+                           to whole 32-bit words, even offset): the pad element is
+                           written and never read. Population planes are rows * pitch
+                           elements apart. */
     double tau;         /* BGK tau / TRT tau_plus */
     double tau_minus;   /* TRT */
 } lgb_batch_domain;
@@ -301,7 +342,8 @@ typedef struct {
     void *f_out;         /* pool written this step (pull pattern) */
     int64_t pool_elements;
     uint32_t *status;    /* optional; bit 0 non-finite density, bit 1 a tile
-                            outside its domain or the pool (skipped) */
+                            outside its domain or the pool, or a pitch the
+                            domain's format does not accept (skipped) */
 } lgb_batch_desc;
 
 /* Host-only: cut every domain into tiles of whole rows holding about

@@ -6,7 +6,8 @@ The public names mirror lettuce's (``Context``, stencils, ``UnitConversion``,
 script written against lettuce's native path runs unchanged. The stepping
 is done by hand-written CUDA kernels in ``liblettuce_gb300.so``, reached
 through its C ABI (include/lettuce_gb300.h); there is no CPU or torch
-fallback for the step.
+fallback for the step. ``native_invoke`` / ``install`` put the same kernels
+behind lettuce's own ``Simulation`` objects (lettuce/_simulation.py:229).
 """
 from ._context import Context
 from ._stencil import D1Q3, D2Q9, D3Q15, D3Q19, D3Q27, Stencil, TorchStencil
@@ -33,6 +34,7 @@ from ._native import NativeBoundary, NativeCollision, NativeEquilibrium
 from ._batched import BatchedSimulation, batched_taylor_green
 from ._adjoint import moments_torch, rollout
 from ._slab import Slab, SlabSimulation, exchange, exchange_local
+from ._lettuce_native import NativeStep, install, native_invoke, native_step
 
 __version__ = "0.1.0"
 
@@ -55,5 +57,6 @@ __all__ = [
     "batched_taylor_green", "rollout", "moments_torch", "Slab", "SlabSimulation",
     "exchange", "exchange_local", "RegularizedCollision", "SmagorinskyCollision", "Force",
     "Guo", "ShanChen", "PoiseuilleFlow2D", "MRTCollision", "Transform", "D1Q3Transform",
-    "D2Q9Dellar", "D2Q9Lallemand", "D3Q27Hermite",
+    "D2Q9Dellar", "D2Q9Lallemand", "D3Q27Hermite", "native_invoke", "native_step", "install",
+    "NativeStep",
 ]

@@ -5,7 +5,10 @@ boundaries) with one BGK or TRT collision each, moves their populations into
 one pooled pair of fields, cuts every domain into tiles of whole rows
 (``lgb_batch_plan``) and advances all of them with one persistent launch per
 step (``lgb_batched_step``, lettuce's PRE_STREAMING order). A run of steps is
-replayed from a captured CUDA graph. Launch shape (threads per block, tile
+replayed from a captured CUDA graph. With the 16-bit shifted storages a
+domain whose rows have an odd length is stored with one pad element per row,
+so that every domain runs the two-cell kernel path; its flow then holds a
+copy of its populations, refreshed after each call. Launch shape (threads per block, tile
 size) is chosen by measurement on first use and cached on disk
 (``lettuce_gb300._autotune``). lettuce itself advances one Flow per
 Simulation; the per-domain arithmetic is the same as ``Simulation``'s.
@@ -24,7 +27,7 @@ from ._collision import BGKCollision, NoCollision, TRTCollision
 
 __all__ = ["BatchedSimulation", "plan_tiles", "batched_taylor_green"]
 
-DOMAIN_DTYPE = np.dtype([("offset", "<i8"), ("res", "<i4", (3,)), ("reserved", "<i4"),
+DOMAIN_DTYPE = np.dtype([("offset", "<i8"), ("res", "<i4", (3,)), ("pitch", "<i4"),
                          ("tau", "<f8"), ("tau_minus", "<f8")])
 POOL_ALIGN = 128  # elements
 TILE_DTYPE = np.dtype([("domain", "<i4"), ("row_begin", "<i4"), ("row_end", "<i4"),
@@ -97,33 +100,41 @@ class BatchedSimulation:
         dom = np.zeros(len(flows), dtype=DOMAIN_DTYPE)
         off = 0
         cells = 0
+        # the 16-bit formats step two cells per 32-bit word: a domain with an
+        # odd row length is stored with one pad element per row so that its
+        # rows are whole words too (the pad is written and never read)
+        pad_odd = self.context.storage in (_lib.F16_SHIFTED, _lib.BF16_SHIFTED)
+        self._pitch = []
         for b, (fl, c) in enumerate(zip(flows, collisions)):
             res = list(fl.resolution) + [1] * (3 - len(fl.resolution))
+            z = int(fl.resolution[-1])
+            pitch = z + 1 if (pad_odd and z % 2 == 1) else z
+            self._pitch.append(pitch)
             # every domain starts on a 128-element boundary of the pool, so the
             # two-cell kernel of the 16-bit formats reads whole aligned words
             off = -(-off // POOL_ALIGN) * POOL_ALIGN
             dom[b]["offset"] = off
             dom[b]["res"] = res
+            dom[b]["pitch"] = pitch
             if isinstance(c, TRTCollision):
                 dom[b]["tau"], dom[b]["tau_minus"] = c.tau_plus, c.tau_minus
             elif isinstance(c, BGKCollision):
                 dom[b]["tau"], dom[b]["tau_minus"] = c.tau, 1.0
             else:
                 dom[b]["tau"], dom[b]["tau_minus"] = 1.0, 1.0
-            off += q * int(np.prod(fl.resolution))
+            off += q * self._alloc_cells(fl, pitch)
             cells += int(np.prod(fl.resolution))
         self.domains = dom
         self.pool_elements = off
         self.n_cells = cells
         dev = self.context.device
         sdt = self.context.storage_dtype
-        self._pools = [torch.empty(off, dtype=sdt, device=dev),
-                       torch.empty(off, dtype=sdt, device=dev)]
+        # zero-filled: pad elements start finite
+        self._pools = [torch.zeros(off, dtype=sdt, device=dev),
+                       torch.zeros(off, dtype=sdt, device=dev)]
         for b, fl in enumerate(flows):
-            n = q * int(np.prod(fl.resolution))
-            o = int(dom[b]["offset"])
             fl._settle()
-            self._pools[0][o:o + n].copy_(fl.f_raw.reshape(-1))
+            self._domain_view(self._pools[0], b).copy_(fl.f_raw)
         self._cur = 0
         self._domains_dev = torch.from_numpy(dom.view(np.uint8).copy()).to(dev)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -226,14 +237,30 @@ class BatchedSimulation:
         self._bind_flows()
         return num_steps * self.n_cells / 1e6 / (end - beg)
 
-    def _bind_flows(self):
-        """point every flow's population tensor at its slice of the current pool"""
-        pool = self._pools[self._cur]
+    @staticmethod
+    def _alloc_cells(flow, pitch: int) -> int:
+        """pool elements per population plane: rows x pitch"""
+        return int(np.prod(flow.resolution[:-1])) * int(pitch)
+
+    def _domain_view(self, pool: torch.Tensor, b: int) -> torch.Tensor:
+        """domain b's populations [Q, *resolution] inside ``pool`` (strided
+        when its rows are padded)"""
+        fl = self.flows[b]
         q = self.stencil.q
+        pitch = self._pitch[b]
+        o = int(self.domains[b]["offset"])
+        n = q * self._alloc_cells(fl, pitch)
+        v = pool[o:o + n].view([q] + list(fl.resolution[:-1]) + [pitch])
+        return v[..., :fl.resolution[-1]]
+
+    def _bind_flows(self):
+        """point every flow's population tensor at its slice of the current
+        pool; a domain stored with padded rows gets a contiguous copy (the
+        flow's kernels read contiguous fields), refreshed after every call"""
+        pool = self._pools[self._cur]
         for b, fl in enumerate(self.flows):
-            n = q * int(np.prod(fl.resolution))
-            o = int(self.domains[b]["offset"])
-            fl._f = pool[o:o + n].view([q] + list(fl.resolution))
+            v = self._domain_view(pool, b)
+            fl._f = v if v.is_contiguous() else v.contiguous()
             fl._aa_pending = False
             fl._stream_pending = None
 

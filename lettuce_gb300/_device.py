@@ -87,6 +87,77 @@ def reduce(stencil_id: int, storage: int, res: Sequence[int], f: torch.Tensor,
     return out
 
 
+def _broadcast_view(t: torch.Tensor, lead: int, res: Sequence[int]) -> torch.Tensor:
+    """``t`` viewed as [lead, *res] with stride 0 on broadcast dimensions (a
+    tensor without the leading dimension gets one)"""
+    full = [lead] + list(res)
+    if t.dim() < len(full):
+        t = t.reshape([1] * (len(full) - t.dim()) + list(t.shape))
+    return t.expand(full)
+
+
+def equilibrium(stencil_id: int, storage: int, res: Sequence[int], rho: torch.Tensor,
+                u: torch.Tensor, f: Optional[torch.Tensor] = None,
+                moments: Optional[tuple] = None):
+    """feq(rho, u) into ``f`` (storage format) and/or its moments into
+    ``moments`` = (rho_out [*res], u_out [D, *res]) in the compute dtype;
+    rho broadcastable to [1, *res], u to [D, *res], both on the device in
+    the compute dtype"""
+    L = _lib.load()
+    d = len(res)
+    rv = _broadcast_view(rho, 1, res)
+    uv = _broadcast_view(u, d, res)
+    for t, what in ((rv, "equilibrium density"), (uv, "equilibrium velocity")):
+        if not t.is_cuda:
+            raise RuntimeError(f"{what}: lettuce_gb300 runs on CUDA tensors only")
+    rs = (ctypes.c_int64 * 3)(*(list(rv.stride()[1:]) + [0] * (3 - d)))
+    us = (ctypes.c_int64 * 4)(*(list(uv.stride()) + [0] * (3 - d)))
+    r3 = _lib.i32x3(res)
+    fptr = None
+    if f is not None:
+        _require_cuda(f, "equilibrium output")
+        fptr = f.data_ptr()
+    rptr = uptr = None
+    if moments is not None:
+        for t in moments:
+            _require_cuda(t, "equilibrium moments")
+        rptr, uptr = moments[0].data_ptr(), moments[1].data_ptr()
+    _lib.check(L.lgb_equilibrium(stencil_id, storage, ctypes.cast(r3, ctypes.c_void_p),
+                                 rv.data_ptr(), ctypes.cast(rs, ctypes.c_void_p), uv.data_ptr(),
+                                 ctypes.cast(us, ctypes.c_void_p), fptr, rptr, uptr,
+                                 stream_of(rv)), "lgb_equilibrium")
+
+
+def init_fneq(stencil_id: int, storage: int, res: Sequence[int], rho: torch.Tensor,
+              u: torch.Tensor, tau: float, f: torch.Tensor):
+    """f = feq(rho, u) - fneq (lettuce's initialize_f_neq) from contiguous
+    rho [*res] / u [D, *res] in the compute dtype, into ``f`` (storage format)"""
+    for t, what in ((rho, "density"), (u, "velocity"), (f, "population field")):
+        _require_cuda(t, f"init_fneq {what}")
+    L = _lib.load()
+    r3 = _lib.i32x3(res)
+    _lib.check(L.lgb_init_fneq(stencil_id, storage, ctypes.cast(r3, ctypes.c_void_p),
+                               rho.data_ptr(), u.data_ptr(), float(tau), f.data_ptr(),
+                               stream_of(f)), "lgb_init_fneq")
+
+
+def enstrophy_lu(u: torch.Tensor) -> torch.Tensor:
+    """float64 device tensor [1]: sum over cells of |curl u|^2 of a velocity
+    field [D, *res] (D = 2 or 3, lattice units, dx = 1)"""
+    _require_cuda(u, "enstrophy")
+    if u.dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"enstrophy: velocity in float32 or float64, not {u.dtype}")
+    L = _lib.load()
+    d = u.shape[0]
+    out = torch.empty(1, dtype=torch.float64, device=u.device)
+    r3 = _lib.i32x3(list(u.shape[1:]))
+    prec = _lib.F64 if u.dtype == torch.float64 else _lib.F32
+    _lib.check(L.lgb_enstrophy(int(d), prec, ctypes.cast(r3, ctypes.c_void_p), u.data_ptr(),
+                               out.data_ptr(), scratch_for(u.device).data_ptr(), stream_of(u)),
+               "lgb_enstrophy")
+    return out
+
+
 def convert(stencil_id: int, src: torch.Tensor, src_storage: int, dst: torch.Tensor,
             dst_storage: int, n_cells: int):
     _require_cuda(src, "convert")

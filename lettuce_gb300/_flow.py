@@ -138,15 +138,51 @@ class Flow(ABC):
 
     def initialize(self):
         """equilibrium initialisation, plus the non-equilibrium part if
-        ``initialize_fneq`` (lettuce/_flow.py:127-143)"""
+        ``initialize_fneq`` (lettuce/_flow.py:127-143). On a CUDA device with
+        the quadratic equilibrium the populations come from the library's
+        initialisation kernels (the equilibrium, then the non-equilibrium
+        part from 6th-order differences of its velocity); elsewhere from the
+        torch expressions."""
         initial_p, initial_u = self.initial_pu()
         initial_rho = self.context.convert_to_tensor(
             self.units.convert_pressure_pu_to_density_lu(initial_p))
         initial_u = self.context.convert_to_tensor(
             self.units.convert_velocity_to_lu(initial_u))
+        if self._initialize_on_device(initial_rho, initial_u):
+            return
         self.f = self.equilibrium(self, rho=initial_rho, u=initial_u)
         if self.initialize_fneq:
             self.f = initialize_f_neq(self)
+
+    def _device_equilibrium(self) -> bool:
+        """the flow's equilibrium is the one the kernels evaluate"""
+        return (self.context.device.type == "cuda"
+                and type(self.equilibrium) in (QuadraticEquilibrium,
+                                               QuadraticEquilibriumLessMemory))
+
+    def _initialize_on_device(self, rho: torch.Tensor, u: torch.Tensor) -> bool:
+        if not self._device_equilibrium() or (self.initialize_fneq and self.stencil.d < 2):
+            return False
+        ctx = self.context
+        res = list(self.resolution)
+        rho = rho.to(device=ctx.device, dtype=ctx.dtype)
+        u = u.to(device=ctx.device, dtype=ctx.dtype)
+        out = torch.empty([self.stencil.q] + res, dtype=ctx.storage_dtype, device=ctx.device)
+        sid = self.stencil.lgb_id
+        if not self.initialize_fneq:
+            _device.equilibrium(sid, ctx.storage, res, rho, u, f=out)
+        else:
+            # lettuce reads rho and u back from the equilibrium it has just
+            # set, then adds the non-equilibrium part (lettuce/_flow.py:341-367)
+            r1 = torch.empty(res, dtype=ctx.dtype, device=ctx.device)
+            u1 = torch.empty([self.stencil.d] + res, dtype=ctx.dtype, device=ctx.device)
+            _device.equilibrium(sid, ctx.storage, res, rho, u, moments=(r1, u1))
+            _device.init_fneq(sid, ctx.storage, res, r1, u1,
+                              self.units.relaxation_parameter_lu, out)
+        self._f = out
+        self._aa_pending = False
+        self._stream_pending = None
+        return True
 
     # -- the population field ---------------------------------------------
     @property
@@ -393,7 +429,15 @@ def initialize_f_neq(flow: Flow) -> torch.Tensor:
     """feq - fneq with the first-order non-equilibrium part
     fneq_i = w_i tau rho S_ab Q_iab / cs^2, Q_iab = e_ia e_ib - cs^2 delta_ab,
     S_ab = d_b u_a by 6th-order differences (Krueger et al. 2017; the same
-    initialisation as lettuce/_flow.py:341-367)."""
+    initialisation as lettuce/_flow.py:341-367). On a CUDA device with the
+    quadratic equilibrium: the moment kernel and the library's fneq kernel."""
+    if flow._device_equilibrium() and flow.stencil.d >= 2:
+        rho, u = flow._own_moments()
+        out = flow.context.empty_tensor([flow.stencil.q] + list(flow.resolution))
+        _device.init_fneq(flow.stencil.lgb_id, _device.storage_of(out.dtype), flow.resolution,
+                          rho.contiguous(), u.contiguous(), flow.units.relaxation_parameter_lu,
+                          out)
+        return out
     f = flow.f
     rho = flow.rho(f)
     u = flow.u(f)

@@ -12,7 +12,7 @@ import threading
 
 from . import build as _build
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 LINK_FORCE_BLOCK = 256  # LGB_LINK_FORCE_BLOCK
 MAX_SUBSTEPS = 8
 REDUCE_FIELDS = 5
@@ -31,7 +31,8 @@ OPT_ONE_CELL, OPT_PUSH_GUARD = 1, 2
 
 EXPORTED = ["lgb_abi_version", "lgb_last_error", "lgb_step", "lgb_moments",
             "lgb_reduce_scratch_bytes", "lgb_reduce", "lgb_reduce_static", "lgb_convert",
-            "lgb_batch_plan", "lgb_batched_step", "lgb_adjoint_step", "lgb_host_pointer"]
+            "lgb_batch_plan", "lgb_batched_step", "lgb_adjoint_step", "lgb_host_pointer",
+            "lgb_equilibrium", "lgb_init_fneq", "lgb_enstrophy"]
 REDUCE_STATIC_SCRATCH_BYTES = 48640
 
 
@@ -127,6 +128,12 @@ def load():
         L.lgb_convert.restype = ctypes.c_int
         L.lgb_host_pointer.argtypes = [P, ctypes.POINTER(ctypes.c_void_p)]
         L.lgb_host_pointer.restype = ctypes.c_int
+        L.lgb_equilibrium.argtypes = [I32, I32, P, P, P, P, P, P, P, P, P]
+        L.lgb_equilibrium.restype = ctypes.c_int
+        L.lgb_init_fneq.argtypes = [I32, I32, P, P, P, ctypes.c_double, P, P]
+        L.lgb_init_fneq.restype = ctypes.c_int
+        L.lgb_enstrophy.argtypes = [I32, I32, P, P, P, P, P]
+        L.lgb_enstrophy.restype = ctypes.c_int
         if L.lgb_abi_version() != ABI_VERSION:
             raise LibraryError(f"{path} has ABI version {L.lgb_abi_version()}, "
                                f"expected {ABI_VERSION}; rebuild it")

@@ -34,6 +34,9 @@ STEP_STENCILS = ["d1q3", "d2q9", "d3q15", "d3q19", "d3q27"]
 # the longest to compile)
 SPLIT_STENCILS = ("d3q19", "d3q27")
 N_STORAGES = 4
+# per-unit flags: the initialisation / enstrophy unit rounds every product
+# and sum on its own (no fused multiply-add), in lettuce's evaluation order
+UNIT_FLAGS = {"lgb_init.cu": ["-fmad=false"]}
 
 
 def nvcc_path() -> str:
@@ -61,7 +64,7 @@ def _units():
                               [f"-DLGB_STORAGE_ID={s}", "-DLGB_EXT_COLLISIONS=1"] + part))
     for src in sorted(os.listdir(CSRC)):
         if src.endswith(".cu") and not src.startswith("lgb_step_"):
-            units.append((src[:-3] + ".o", src, []))
+            units.append((src[:-3] + ".o", src, UNIT_FLAGS.get(src, [])))
     return units
 
 

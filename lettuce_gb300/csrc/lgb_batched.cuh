@@ -5,9 +5,11 @@
 // kernel's resident blocks walk the tile table with a grid stride, one cell
 // per thread, pulling from the periodic neighbours inside the tile's domain.
 // The per-domain relaxation times come from the domain table. Domains of the
-// 16-bit formats with an even row length (and a word-aligned offset) run the
-// two-cell step (one 32-bit word per population pair, lgb_step_vec.cuh),
-// bit-identical to the one-cell step.
+// 16-bit formats whose rows are whole 32-bit words -- an even row length, or
+// an odd one stored with one pad element per row (pitch = length + 1) --
+// and whose offset is word-aligned run the two-cell step (one 32-bit word
+// per population pair, lgb_step_vec.cuh), bit-identical to the one-cell
+// step.
 #pragma once
 
 #include "lgb_shifted.cuh"
@@ -15,6 +17,60 @@
 #include "lgb_step_vec.cuh"
 
 namespace lgb {
+
+// the pulled pair (z0 + dz, z0 + 1 + dz) of a row of Zh words whose last
+// word holds (cell Z - 1, pad): the periodic wrap skips the pad element
+__device__ __forceinline__ uint32_t load_pair_padded(const uint32_t *__restrict__ row, uint32_t tz,
+                                                     uint32_t Zh, int dz) {
+    if (dz == 0) return __ldg(row + tz);
+    if (dz < 0) {
+        // (cell 2 tz - 1, cell 2 tz); left of cell 0 is cell Z - 1, the low
+        // half of the last word
+        if (tz == 0) return __byte_perm(__ldg(row + Zh - 1), __ldg(row), 0x5410);
+        return __byte_perm(__ldg(row + tz - 1), __ldg(row + tz), 0x5432);
+    }
+    // (cell 2 tz + 1, cell 2 tz + 2); right of cell Z - 1 is cell 0 (the
+    // last pair's second lane is the pad and takes cell 1)
+    if (tz + 1 == Zh) return __ldg(row);
+    return __byte_perm(__ldg(row + tz), __ldg(row + tz + 1), 0x5432);
+}
+
+// the pull step of pair tz of row (x, y) in a domain whose rows are padded
+// to Zh words (odd row length p.Z, pitch p.Z + 1, Nh words per population
+// plane); the pad lane is computed and stored but never read by a real cell
+// and is left out of the status check
+template <int SID, int ST, int COLL>
+__device__ __forceinline__ void step_pair_padded_pull(const StepParams &p, const uint32_t tz,
+                                                      const uint32_t x, const uint32_t y,
+                                                      const uint32_t Zh, const uint32_t Nh) {
+    using S = Stencil<SID>;
+    using P = Pack16<ST>;
+    const uint32_t row = x * p.Y + y;
+    const uint32_t xm = x == 0 ? p.X - 1 : x - 1, xp = x + 1 == p.X ? 0 : x + 1;
+    const uint32_t ym = y == 0 ? p.Y - 1 : y - 1, yp = y + 1 == p.Y ? 0 : y + 1;
+    const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in);
+    auto row_of = [&](int dx, int dy) -> uint32_t {
+        const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
+        const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
+        return (a * p.Y + b) * Zh;
+    };
+    float2 h[S::Q];
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) {
+        const uint32_t *r = fin + (size_t)q * Nh + row_of(-ix<S>(q), -iy<S>(q));
+        h[q] = P::decode(load_pair_padded(r, tz, Zh, -iz<S>(q)));
+    }
+    collide_shifted<S, Lane2, COLL>(h, p.cp);
+    if (p.status) {
+        float2 r = h[0];
+#pragma unroll
+        for (int q = 1; q < S::Q; ++q) r = Lane2::add(r, h[q]);
+        if (!isfinite(r.x) || (tz + 1 < Zh && !isfinite(r.y))) atomicOr(p.status, 1u);
+    }
+    uint32_t *fout = static_cast<uint32_t *>(p.f_out);
+#pragma unroll
+    for (int q = 0; q < S::Q; ++q) fout[(size_t)q * Nh + row * Zh + tz] = P::encode(h[q]);
+}
 
 struct BatchParams {
     const void *f_in;
@@ -54,9 +110,16 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
         }
         g.X = r[0]; g.Y = r[1]; g.Z = r[2];
         const uint64_t n64 = (uint64_t)r[0] * r[1] * r[2];
+        // row pitch: the row length, or (16-bit shifted formats, odd row
+        // length) one more, a pad element per row
+        const uint32_t pitch = dom.pitch == 0 ? r[2] : (uint32_t)dom.pitch;
+        const bool padded = pitch != r[2];
+        ok = ok && dom.pitch >= 0 &&
+             (!padded || (HSPACE && (r[2] & 1u) && pitch == r[2] + 1 && (dom.offset & 1) == 0));
+        const uint64_t n_alloc = (uint64_t)r[0] * r[1] * pitch;
         // the tile must lie inside its domain and the domain inside the pool
-        ok = ok && n64 < (1ull << 32) && dom.offset >= 0 &&
-             (uint64_t)dom.offset + (uint64_t)S::Q * n64 <= (uint64_t)p.pool_elements &&
+        ok = ok && n_alloc < (1ull << 32) && dom.offset >= 0 &&
+             (uint64_t)dom.offset + (uint64_t)S::Q * n_alloc <= (uint64_t)p.pool_elements &&
              tile.row_begin >= 0 && tile.row_begin <= tile.row_end &&
              (uint64_t)tile.row_end <= (uint64_t)r[0] * r[1] && dom.tau > 0.0;
         if (!ok) {
@@ -76,6 +139,30 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
         // of fast-division constants derived per tile)
         const uint32_t step = blockDim.x;
         if constexpr (HSPACE) {
+            if (padded) {
+                g.f_in = fin;
+                g.f_out = fout;
+                g.cp = cp;
+                g.status = p.status;
+                const uint32_t Zh = pitch >> 1;
+                const uint32_t Nh = (uint32_t)(n_alloc >> 1);
+                const uint32_t end = (uint32_t)tile.row_end * Zh;
+                uint32_t t2 = (uint32_t)tile.row_begin * Zh + threadIdx.x;
+                if (t2 >= end) continue;
+                uint32_t row = t2 / Zh, tz = t2 - row * Zh;
+                uint32_t x = row / g.Y, y = row - x * g.Y;
+                while (true) {
+                    step_pair_padded_pull<SID, ST, COLL>(g, tz, x, y, Zh, Nh);
+                    t2 += step;
+                    if (t2 >= end) break;
+                    tz += step;
+                    while (tz >= Zh) {
+                        tz -= Zh;
+                        if (++y == g.Y) { y = 0; ++x; }
+                    }
+                }
+                continue;
+            }
             if ((g.Z & 1u) == 0 && (dom.offset & 1) == 0) {
                 g.f_in = fin;
                 g.f_out = fout;
