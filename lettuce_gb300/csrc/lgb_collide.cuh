@@ -141,18 +141,29 @@ template <class S> LGB_HD constexpr int q_of(int x, int y, int z) {
     return -1;
 }
 
+// Where a collision reads and writes a cell's populations: a register array
+// (RegPops), or a column of a block's shared-memory stage (lgb_step.cuh,
+// StagePops) read back for every pass instead of being held in registers.
+// Both evaluate the same operations in the same order.
+template <class R, int Q> struct RegPops {
+    R (&f)[Q];
+    LGB_HD R get(int q) const { return f[q]; }
+    LGB_HD void set(int q, R v) const { f[q] = v; }
+};
+
 // D3Q27: density, momentum and the second moments m_ab = sum_q e_qa e_qb f_q
 // (packed xx, yy, zz, xy, xz, yz) from partial sums along the nine z-lines
 // (about 70 additions instead of about 180 for the ten sums taken one by one)
-template <class S, class R>
-LGB_HD void moments27(const R (&f)[S::Q], R &rho, R (&j)[3], R (&m)[6]) {
+template <class S, class R, class P>
+LGB_HD void moments27_of(const P &f, R &rho, R (&j)[3], R (&m)[6]) {
     static_assert(S::Q == 27, "D3Q27 only");
     R A[3][3], B[3][3], C[3][3];  // per (x, y) line: sum f, sum z f, sum z^2 f
 #pragma unroll
     for (int x = -1; x <= 1; ++x) {
 #pragma unroll
         for (int y = -1; y <= 1; ++y) {
-            const R lo = f[q_of<S>(x, y, -1)], mid = f[q_of<S>(x, y, 0)], hi = f[q_of<S>(x, y, 1)];
+            const R lo = f.get(q_of<S>(x, y, -1)), mid = f.get(q_of<S>(x, y, 0)),
+                    hi = f.get(q_of<S>(x, y, 1));
             C[x + 1][y + 1] = hi + lo;
             B[x + 1][y + 1] = hi - lo;
             A[x + 1][y + 1] = C[x + 1][y + 1] + mid;
@@ -179,6 +190,12 @@ LGB_HD void moments27(const R (&f)[S::Q], R &rho, R (&j)[3], R (&m)[6]) {
     m[5] = Byp - Bym;
 }
 
+template <class S, class R>
+LGB_HD void moments27(const R (&f)[S::Q], R &rho, R (&j)[3], R (&m)[6]) {
+    R(&fm)[S::Q] = const_cast<R(&)[S::Q]>(f);
+    moments27_of<S>(RegPops<R, S::Q>{fm}, rho, j, m);
+}
+
 // Entropic KBC collision (lettuce/ext/_collision/kbc_collision.py:96-160),
 // D3Q27 and D2Q9. The shear part delta_s = s(f) - s(feq) is linear in the
 // second moments, s(.) of kbc_collision.py:44-94; for the quadratic
@@ -188,18 +205,21 @@ LGB_HD void moments27(const R (&f)[S::Q], R &rho, R (&j)[3], R (&m)[6]) {
 //   delta_h = f - feq - delta_s,
 //   gamma = 1/beta - (2 - 1/beta) <delta_s delta_h / feq> / <delta_h^2 / feq>
 // (2 where that is below 1e-15 or NaN) and f <- f - beta (2 delta_s + gamma delta_h).
-template <class S, class R>
-LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+template <class S, class R, class P>
+LGB_HD void collide_kbc_of(const P &f, const CollideParams &cp, R &rho_out) {
     static_assert(S::Q == 27 || S::Q == 9, "KBC is defined for D3Q27 and D2Q9");
     R rho, u[3];
     R m27[6];
     if constexpr (S::Q == 27) {
-        moments27<S>(f, rho, u, m27);
+        moments27_of<S>(f, rho, u, m27);
         const R inv = R(1) / rho;
 #pragma unroll
         for (int d = 0; d < 3; ++d) u[d] *= inv;
     } else {
-        cell_moments<S>(f, rho, u);
+        R fr[S::Q];
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) fr[q] = f.get(q);
+        cell_moments<S>(fr, rho, u);
     }
     const R uu = dot_uu<S>(u);
     const R inv_rho = R(1) / rho;
@@ -230,9 +250,9 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             const int ex = S::e(q, 0), ey = S::e(q, 1);
-            if (ex) mxx += f[q];
-            if (ey) myy += f[q];
-            if (ex * ey == 1) mxy += f[q]; else if (ex * ey == -1) mxy -= f[q];
+            if (ex) mxx += f.get(q);
+            if (ey) myy += f.get(q);
+            if (ex * ey == 1) mxy += f.get(q); else if (ex * ey == -1) mxy -= f.get(q);
         }
         const R dxx = mxx * inv_rho - (third + u[0] * u[0]);
         const R dyy = myy * inv_rho - (third + u[1] * u[1]);
@@ -290,7 +310,7 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     R sum_s, sum_h;
     {
         const R d_s = ds(0);
-        const R dh = f[0] - feq0 - d_s;
+        const R dh = f.get(0) - feq0 - d_s;
         const R ifeq = kbc_rcp(feq0);
         sum_s = d_s * dh * ifeq;
         sum_h = dh * dh * ifeq;
@@ -302,7 +322,7 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
         R fq, fo;
         feq_pair(q, fq, fo);
         const R d_s = ds(q);
-        const R hq = f[q] - fq - d_s, ho = f[o] - fo - d_s;
+        const R hq = f.get(q) - fq - d_s, ho = f.get(o) - fo - d_s;
         const R iq = kbc_rcp(fq), io = kbc_rcp(fo);
         sum_s += d_s * (hq * iq + ho * io);
         sum_h += hq * hq * iq + ho * ho * io;
@@ -315,7 +335,8 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
     const R b2 = R(2) * beta, bg = beta * gamma;
     {
         const R d_s = ds(0);
-        f[0] = f[0] - b2 * d_s - bg * (f[0] - feq0 - d_s);
+        const R f0 = f.get(0);
+        f.set(0, f0 - b2 * d_s - bg * (f0 - feq0 - d_s));
     }
 #pragma unroll
     for (int q = 1; q < S::Q; ++q) {
@@ -324,11 +345,17 @@ LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
         R fq, fo;
         feq_pair(q, fq, fo);
         const R d_s = ds(q);
-        const R hq = f[q] - fq - d_s, ho = f[o] - fo - d_s;
-        f[q] = f[q] - b2 * d_s - bg * hq;
-        f[o] = f[o] - b2 * d_s - bg * ho;
+        const R gq = f.get(q), go = f.get(o);
+        const R hq = gq - fq - d_s, ho = go - fo - d_s;
+        f.set(q, gq - b2 * d_s - bg * hq);
+        f.set(o, go - b2 * d_s - bg * ho);
     }
     rho_out = rho;
+}
+
+template <class S, class R>
+LGB_HD void collide_kbc(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {
+    collide_kbc_of<S>(RegPops<R, S::Q>{f}, cp, rho_out);
 }
 
 // j / rho + ueq_scale a / rho (forced BGK and Smagorinsky,

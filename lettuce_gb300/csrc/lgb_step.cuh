@@ -283,6 +283,33 @@ __device__ __forceinline__ void store_value(typename Sto::T *ptr, typename Sto::
     else Sto::store(ptr, v, w);
 }
 
+// D3Q27 KBC in float32 with the pulling / collide-only patterns: the cell's 27
+// populations go through a shared-memory stage (one column per thread,
+// [Q][256], consecutive threads in consecutive banks) and the collision reads
+// them back for each of its passes (moments, entropic sums, update) instead
+// of holding them in registers across the passes. Same operations in the
+// same order as the register form; the registers freed raise the resident
+// blocks per SM.
+#ifndef LGB_KBC_STAGE
+#define LGB_KBC_STAGE 1
+#endif
+constexpr int kStageThreads = 256;
+template <int SID, int ST, int COLL, int PAT, int MASK>
+__host__ __device__ constexpr bool kbc_staged() {
+    return LGB_KBC_STAGE && SID == LGB_D3Q27 && COLL == LGB_KBC && ST == LGB_F32 &&
+           (PAT == LGB_PULL || PAT == LGB_LOCAL) && (MASK == 0 || MASK == 1 || MASK == 3);
+}
+
+template <class R> struct StagePops {
+    R *col;
+    __device__ __forceinline__ R get(int q) const {
+        return *reinterpret_cast<volatile R *>(col + q * kStageThreads);
+    }
+    __device__ __forceinline__ void set(int q, R v) const {
+        *reinterpret_cast<volatile R *>(col + q * kStageThreads) = v;
+    }
+};
+
 // MASK: 0 = no boundaries; 1 = boundaries, every cell except those of the
 // anti-bounce-back outlet plane (when there is one); 2 = the outlet plane
 // only (one thread per plane cell); 3 and 4 = 1 and 2 with bounce-back links
@@ -343,6 +370,36 @@ __device__ __forceinline__ void step_cell(const StepParams &p, const TT &tab) {
     }
     R f[S::Q];
     load_cell<S, Sto, LOAD, MASKED, HSPACE, LINKS>(p, fin, c, n, nsbits, f, lbits);
+
+    if constexpr (kbc_staged<SID, ST, COLL, PAT, MASK>()) {
+        // (each thread reads and writes only its own column: no barrier)
+        __shared__ R stage[S::Q * kStageThreads];
+        const StagePops<R> sp{stage + threadIdx.x};
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) sp.set(q, f[q]);
+        const int idx = fl & LGB_FLAG_INDEX_MASK;
+        if (!BULK || idx == p.coll_idx) {
+            R r;
+            collide_kbc_of<S>(sp, p.cp, r);
+        } else {
+            R g[S::Q];
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) g[q] = sp.get(q);
+            apply_local_substep<S, COLL, false>(p, select_sub(p, idx), c, g, tab);
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) sp.set(q, g[q]);
+        }
+        const size_t N = p.N;
+        R r = R(0);
+#pragma unroll
+        for (int q = 0; q < S::Q; ++q) {
+            const R v = sp.get(q);
+            r += v;
+            store_value<Sto, false>(fout + (size_t)q * N + n, v, S::w(q));
+        }
+        if (p.status && !isfinite(r)) atomicOr(p.status, 1u);
+        return;
+    }
 
     if constexpr (HSPACE) {
         if constexpr (PAT != LGB_STREAM_ONLY && PAT != LGB_AA_UNPACK)
@@ -437,8 +494,18 @@ step_kernel(const __grid_constant__ StepParams p, const __grid_constant__ StepTa
 #ifndef LGB_KBC_PUSH_MIN_BLOCKS
 #define LGB_KBC_PUSH_MIN_BLOCKS 3
 #endif
+// the staged float32 kernels (27.6 KB of shared memory per block)
+#ifndef LGB_KBC_STAGE_MIN_BLOCKS
+#define LGB_KBC_STAGE_MIN_BLOCKS 4
+#endif
 template <int SID, int ST, int COLL, int PAT, int MASK>
-__global__ void __launch_bounds__(256, PAT == LGB_PUSH ? LGB_KBC_PUSH_MIN_BLOCKS : LGB_KBC_MIN_BLOCKS)
+constexpr int kbc_min_blocks() {
+    return kbc_staged<SID, ST, COLL, PAT, MASK>()
+               ? LGB_KBC_STAGE_MIN_BLOCKS
+               : (PAT == LGB_PUSH ? LGB_KBC_PUSH_MIN_BLOCKS : LGB_KBC_MIN_BLOCKS);
+}
+template <int SID, int ST, int COLL, int PAT, int MASK>
+__global__ void __launch_bounds__(256, (kbc_min_blocks<SID, ST, COLL, PAT, MASK>()))
 step_kernel_bounded(const __grid_constant__ StepParams p,
                     const __grid_constant__ StepTables<SID, ST, COLL> tab) {
     step_cell<SID, ST, COLL, PAT, MASK>(p, tab);

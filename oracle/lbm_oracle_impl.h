@@ -9,6 +9,10 @@ typedef struct {
     int ix[27], iy[27], iz[27]; /* velocities in the internal view */
     int32_t res[3];
     int64_t lstride[3];
+    /* the KBC moment tensor e_x^a e_y^b e_z^c of every velocity
+     * (kbc_collision.py:22-39), [a*9 + b*3 + c][q] in 3-D, [a*3 + b][q] in
+     * 2-D; integer powers of -1, 0, 1, exact in floating point */
+    REAL kbc_m[27][27];
 } SFX(geom);
 
 static int SFX(make_geom)(int stencil, const int32_t *res, SFX(geom) *g)
@@ -26,6 +30,20 @@ static int SFX(make_geom)(int stencil, const int32_t *res, SFX(geom) *g)
     }
     int64_t s = 1;
     for (int i = st->d - 1; i >= 0; --i) { g->lstride[i] = s; s *= res[i]; }
+    for (int k = 0; k < 27; ++k)
+        for (int qi = 0; qi < 27; ++qi) g->kbc_m[k][qi] = 0;
+    if (st->d == 3 && st->q == 27) {
+        for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) for (int c = 0; c < 3; ++c)
+            for (int qi = 0; qi < 27; ++qi)
+                g->kbc_m[a * 9 + b * 3 + c][qi] = (REAL)(pow((REAL)st->e[qi][0], a) *
+                                                         pow((REAL)st->e[qi][1], b) *
+                                                         pow((REAL)st->e[qi][2], c));
+    } else if (st->d == 2 && st->q == 9) {
+        for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b)
+            for (int qi = 0; qi < 9; ++qi)
+                g->kbc_m[a * 3 + b][qi] = (REAL)(pow((REAL)st->e[qi][0], a) *
+                                                 pow((REAL)st->e[qi][1], b));
+    }
     return 0;
 }
 
@@ -69,11 +87,8 @@ static void SFX(kbc_s)(const SFX(geom) *g, const REAL *fc, REAL *s)
         REAL m[3][3][3];
         for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) for (int c = 0; c < 3; ++c) {
             REAL acc = 0;
-            for (int q = 0; q < 27; ++q) {
-                REAL ex = (REAL)g->st->e[q][0], ey = (REAL)g->st->e[q][1], ez = (REAL)g->st->e[q][2];
-                REAL mm = (REAL)(pow(ex, a) * pow(ey, b) * pow(ez, c));
-                acc += mm * fc[q];
-            }
+            const REAL *mrow = g->kbc_m[a * 9 + b * 3 + c];
+            for (int q = 0; q < 27; ++q) acc += mrow[q] * fc[q];
             m[a][b][c] = acc;
         }
         REAL rho = m[0][0][0];
@@ -98,10 +113,8 @@ static void SFX(kbc_s)(const SFX(geom) *g, const REAL *fc, REAL *s)
         REAL m[3][3];
         for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) {
             REAL acc = 0;
-            for (int q = 0; q < 9; ++q) {
-                REAL ex = (REAL)g->st->e[q][0], ey = (REAL)g->st->e[q][1];
-                acc += (REAL)(pow(ex, a) * pow(ey, b)) * fc[q];
-            }
+            const REAL *mrow = g->kbc_m[a * 3 + b];
+            for (int q = 0; q < 9; ++q) acc += mrow[q] * fc[q];
             m[a][b] = acc;
         }
         REAL rho = m[0][0];

@@ -97,7 +97,9 @@ def test_enstrophy_kernel(lgb, dtype):
     for tag, S, n in [("2d", lt.D2Q9, 16), ("3d", lt.D3Q19, 8)]:
         flow = lt.TaylorGreenVortex(lt.Context("cuda:0", dtype), n, 1000, 0.05, S)
         got = lt.Enstrophy(flow)().item()
-        assert abs(got / z[f"{tag}_enstrophy"] - 1) < (1e-12 if dtype == F64 else 1e-6), tag
+        # float32: the velocity itself carries ~1e-7 relative rounding, which
+        # the differences of a smooth field amplify
+        assert abs(got / z[f"{tag}_enstrophy"] - 1) < (1e-12 if dtype == F64 else 1e-5), tag
     # a non-square, random velocity field against the torch expression
     flow = lt.TaylorGreenVortex(lt.Context("cuda:0", F64), [14, 9, 11], 1000, 0.05, lt.D3Q19)
     g = torch.Generator().manual_seed(2)
