@@ -444,15 +444,24 @@ def time_bounce_back_obstacle(lt, torch, device, peak, g, steps, warmup):
 
 
 def config3_long_run(lt, torch, device, peak, steps=5000):
-    """config 3 over its full 5000 steps: the D3Q27 KBC channel 512x128x128
-    (sphere of diameter 24 as lettuce's full-way bounce-back, equilibrium
-    inlet, anti-bounce-back outlet, Re 300, float32, PRE streaming) with its
-    status word (bit 0: a non-finite density) and the mass change; then the
-    same channel with the sphere as the example project's halfway
-    bounce-back computing the momentum exchange every step, its drag and
-    lift coefficients sampled every 100 steps over the last 1000 (the
-    example's F / (0.5 rho_mean u^2 pi r^2), r = 12)"""
+    """config 3 over its full 5000 steps, D3Q27 KBC channel 512x128x128,
+    sphere of diameter 24, equilibrium velocity inlet, Re 300, float32, PRE
+    streaming, with two outflow boundaries:
+
+    * lettuce's Obstacle as it stands (anti-bounce-back outlet): the status
+      word (bit 0: a non-finite density) is read every 250 steps. This flow
+      diverges at the outlet in lettuce's own algorithm: the oracle (its
+      float64 restatement) at a quarter of the size blows up next to the
+      outlet plane within 600 steps, and tests/test_gpu_config3.py holds the
+      kernels to the oracle through the onset;
+    * the same channel with lettuce's pressure outlet (EquilibriumOutletP,
+      rho 1; obstacle.py:119-120 offers it): status, mass change and speed
+      over the whole run; then with the sphere as the example project's
+      halfway bounce-back computing the momentum exchange every step, its
+      drag and lift coefficients sampled every 100 steps over the last 1000
+      (the example's F / (0.5 rho_mean u^2 pi r^2), r = 12)"""
     import math
+    from lettuce_gb300._reporter import reduce_flow
     g = 256
     res = [2 * g, g // 2, g // 2]
     n = int(np.prod(res))
@@ -461,16 +470,47 @@ def config3_long_run(lt, torch, device, peak, steps=5000):
     grid = np.meshgrid(*[np.arange(k) for k in res], indexing="ij", sparse=True)
     solid = sum((gi - ci) ** 2 for gi, ci in zip(grid, centre)) < r * r
     out = {"workload": "D3Q27 KBC obstacle 512x128x128, float32, 5000 steps", "steps": steps}
+    stream = torch.cuda.current_stream(device)
 
-    flow = lt.Obstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
-                       res[0] / 24.0, stencil=lt.D3Q27)
-    flow.mask = solid
-    flow.initialize()
+    class ObstacleP(lt.Obstacle):
+        """lettuce's Obstacle with its pressure outlet instead of the
+        anti-bounce-back outlet"""
+        @property
+        def post_boundaries(self):
+            b = lt.Obstacle.post_boundaries.fget(self)
+            return [b[0], lt.EquilibriumOutletP(self._unit_vector().tolist(), self,
+                                                rho_outlet=1.0), b[2]]
+
+    def make(cls):
+        flow = cls(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                   res[0] / 24.0, stencil=lt.D3Q27)
+        flow.mask = solid
+        flow.initialize()
+        return flow
+
+    # lettuce's Obstacle (anti-bounce-back outlet)
+    flow = make(lt.Obstacle)
     sim = lt.Simulation(flow, lt.KBCCollision(), [],
                         streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
-    from lettuce_gb300._reporter import reduce_flow
-    m0 = reduce_flow(flow)
-    stream = torch.cuda.current_stream(device)
+    first_bad = None
+    for k in range(steps // 250):
+        sim(250)
+        if sim.status:
+            first_bad = (k + 1) * 250
+            break
+    out["anti_bounce_back_outlet"] = {
+        "status": sim.status, "nonfinite_by_step": first_bad,
+        "checked": "status word every 250 steps",
+        "note": "diverges at the outlet in lettuce's algorithm as well (the float64 oracle "
+                "at 128x32x32 blows up next to the outlet within 600 steps)"}
+    del sim, flow
+    torch.cuda.empty_cache()
+
+    # pressure outlet
+    flow = make(ObstacleP)
+    sim = lt.Simulation(flow, lt.KBCCollision(), [],
+                        streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+    m0 = reduce_flow(flow).cpu().numpy()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(device)
     start.record(stream)
@@ -478,26 +518,24 @@ def config3_long_run(lt, torch, device, peak, steps=5000):
     end.record(stream)
     torch.cuda.synchronize(device)
     ms = start.elapsed_time(end) / steps
-    m1 = reduce_flow(flow)
-    m0, m1 = m0.cpu().numpy(), m1.cpu().numpy()
-    umax = float(np.sqrt(m1[2]))
-    out["full_way_bounce_back"] = {
+    m1 = reduce_flow(flow).cpu().numpy()
+    out["pressure_outlet"] = {
         "status": sim.status, "nonfinite_cells": int(m1[3]),
-        "mass_rel_change": float(m1[0] / m0[0] - 1), "max_u_lu": round(umax, 5),
+        "mass_rel_change": float(m1[0] / m0[0] - 1), "max_u_lu": round(float(np.sqrt(m1[2])), 5),
         "ms_per_step": round(ms, 4), "mlups": round(n / (ms * 1e-3) / 1e6, 1),
         "frac_of_peak": round(217 * n / (ms * 1e-3) / 1e9 / peak, 4)}
     del sim, flow
     torch.cuda.empty_cache()
 
-    class EbbObstacle(lt.Obstacle):
+    class EbbObstacleP(ObstacleP):
         psb = ()
 
         @property
         def post_streaming_boundaries(self):
             return list(self.psb)
 
-    flow = EbbObstacle(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
-                       res[0] / 24.0, stencil=lt.D3Q27)
+    flow = EbbObstacleP(lt.Context(device, torch.float32), res, 300, 0.05 * math.sqrt(3),
+                        res[0] / 24.0, stencil=lt.D3Q27)
     flow.initialize()
     sbd = lt.SolidBoundaryData()
     sbd.solid_mask = solid
@@ -513,7 +551,7 @@ def config3_long_run(lt, torch, device, peak, steps=5000):
         sim(100)
         cd.append(float(drag()))
         cl.append(float(lift()))
-    out["halfway_bounce_back"] = {
+    out["pressure_outlet_halfway_bounce_back"] = {
         "status": sim.status, "drag_coefficient": round(float(np.mean(cd)), 4),
         "drag_coefficient_range": [round(min(cd), 4), round(max(cd), 4)],
         "lift_coefficient": round(float(np.mean(cl)), 4),

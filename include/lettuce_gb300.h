@@ -311,11 +311,12 @@ typedef struct {
     int64_t offset;     /* element offset of the domain's [Q][rows * pitch] field in the pool */
     int32_t res[3];     /* lettuce resolution; unused trailing dims = 1 */
     int32_t pitch;      /* elements from one row (last lettuce dimension) to the next;
-                           0 = the row length. The 16-bit shifted formats accept an odd
-                           row length stored with pitch = length + 1 (every row padded
-                           to whole 32-bit words, even offset): the pad element is
-                           written and never read. Population planes are rows * pitch
-                           elements apart. */
+                           0 = the row length. With the 16-bit shifted formats every
+                           row must be whole 32-bit words and the offset even: an odd
+                           row length is stored with pitch = length + 1 (the pad
+                           element is written and never read); other domains of these
+                           formats are skipped with status bit 1. Population planes
+                           are rows * pitch elements apart. */
     double tau;         /* BGK tau / TRT tau_plus */
     double tau_minus;   /* TRT */
 } lgb_batch_domain;

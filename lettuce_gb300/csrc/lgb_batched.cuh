@@ -83,8 +83,22 @@ struct BatchParams {
     uint32_t *status;
 };
 
+// registers of the 16-bit two-dimensional batches (every domain on a pair
+// step): the compiler takes 59-64, which leaves half the warps of an SM idle;
+// 0 = the compiler's choice
+#ifndef LGB_BATCHED_16BIT_2D_MAXREG
+#define LGB_BATCHED_16BIT_2D_MAXREG 48
+#endif
+template <int SID, int ST>
+constexpr int batched_maxreg() {
+    return (LGB_BATCHED_16BIT_2D_MAXREG > 0 && is_shifted<ST>() &&
+            (SID == LGB_D2Q9 || SID == LGB_D1Q3))
+               ? LGB_BATCHED_16BIT_2D_MAXREG : 128;
+}
+
 template <int SID, int ST, int COLL>
-__global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) {
+__global__ void __launch_bounds__(512) __maxnreg__((batched_maxreg<SID, ST>()))
+batched_step_kernel(const BatchParams p) {
     using S = Stencil<SID>;
     using Sto = Storage<ST>;
     using R = typename Sto::R;
@@ -186,6 +200,11 @@ __global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) 
                 }
                 continue;
             }
+            // rows that are not whole 32-bit words (an odd length stored
+            // without its pad, or an odd offset) have no two-cell step:
+            // flagged and skipped (the host pads every odd row)
+            if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
+            continue;
         }
         const uint32_t end = (uint32_t)tile.row_end * g.Z;
         uint32_t n = (uint32_t)tile.row_begin * g.Z + threadIdx.x;

@@ -291,7 +291,7 @@ __device__ __forceinline__ void store_value(typename Sto::T *ptr, typename Sto::
 // same order as the register form; the registers freed raise the resident
 // blocks per SM.
 #ifndef LGB_KBC_STAGE
-#define LGB_KBC_STAGE 1
+#define LGB_KBC_STAGE 0
 #endif
 constexpr int kStageThreads = 256;
 template <int SID, int ST, int COLL, int PAT, int MASK>

@@ -84,3 +84,23 @@ def test_invalid_tile_is_skipped_and_flagged(lgb):
     sim._tiles_dev = torch.from_numpy(tiles.view(np.uint8).reshape(-1)).cuda()
     sim(1, use_graph=False)
     assert sim.status & 2
+
+
+def test_unpadded_odd_rows_of_16bit_batches_are_refused(lgb):
+    """16-bit batches step two cells per 32-bit word: a domain whose odd rows
+    are not padded (pitch 0 in place of length + 1) is skipped with status
+    bit 1, and the other domains still step exactly as alone"""
+    flows, colls = _batch("fp16_shifted", n=3, seed=5, lo=9, hi=30)
+    singles, scolls = _batch("fp16_shifted", n=3, seed=5, lo=9, hi=30)
+    sim = lt.BatchedSimulation(flows, colls, tile_cells=300, threads=128)
+    odd = [b for b, fl in enumerate(flows) if fl.resolution[-1] % 2 == 1]
+    even = [b for b, fl in enumerate(flows) if fl.resolution[-1] % 2 == 0]
+    assert odd and even, [fl.resolution for fl in flows]
+    dom = sim.domains.copy()
+    dom["pitch"][odd[0]] = 0
+    sim._domains_dev = torch.from_numpy(dom.view(np.uint8).copy()).cuda()
+    sim(3, use_graph=False)
+    assert sim.status & 2
+    for b in even:
+        lt.Simulation(singles[b], scolls[b], [], lt.StreamingStrategy.PRE_STREAMING)(3)
+        assert torch.equal(flows[b].f_raw, singles[b].f_raw)
