@@ -90,8 +90,12 @@ def test_unpadded_odd_rows_of_16bit_batches_are_refused(lgb):
     """16-bit batches step two cells per 32-bit word: a domain whose odd rows
     are not padded (pitch 0 in place of length + 1) is skipped with status
     bit 1, and the other domains still step exactly as alone"""
-    flows, colls = _batch("fp16_shifted", n=3, seed=5, lo=9, hi=30)
-    singles, scolls = _batch("fp16_shifted", n=3, seed=5, lo=9, hi=30)
+    # the first seed whose three domains have odd and even row lengths
+    seed = next(s for s in range(100)
+                if len({int(z) % 2 for z in
+                        np.random.default_rng(s).integers(9, 31, size=(3, 2))[:, 1]}) == 2)
+    flows, colls = _batch("fp16_shifted", n=3, seed=seed, lo=9, hi=30)
+    singles, scolls = _batch("fp16_shifted", n=3, seed=seed, lo=9, hi=30)
     sim = lt.BatchedSimulation(flows, colls, tile_cells=300, threads=128)
     odd = [b for b, fl in enumerate(flows) if fl.resolution[-1] % 2 == 1]
     even = [b for b, fl in enumerate(flows) if fl.resolution[-1] % 2 == 0]
