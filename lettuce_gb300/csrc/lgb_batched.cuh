@@ -97,6 +97,7 @@ batched_step_kernel(const BatchParams p) {
     constexpr bool HSPACE = is_shifted<ST>() && shifted_collision<COLL>();
     const T *__restrict__ pool_in = static_cast<const T *>(p.f_in);
     T *pool_out = static_cast<T *>(p.f_out);
+    __shared__ double s_rates[3];
     for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
         const lgb_batch_tile tile = p.tiles[t];
         if (tile.domain < 0 || tile.domain >= p.n_domains) {
@@ -132,11 +133,23 @@ batched_step_kernel(const BatchParams p) {
             continue;
         }
         g.N = (uint32_t)n64;
+        // the domain's relaxation rates, three float64 divisions: one thread
+        // forms them and the block reads them from shared memory (formed by
+        // every thread they kept the float64 pipe busy for a fifth of the
+        // launch). Every thread of the block walks the same tile, so the
+        // branches above are uniform and every thread reaches both barriers.
+        __syncthreads();  // the previous tile's rates have been read
+        if (threadIdx.x == 0) {
+            s_rates[0] = 1.0 / dom.tau;
+            s_rates[1] = 1.0 / (2.0 * dom.tau);
+            s_rates[2] = 1.0 / (2.0 * dom.tau_minus);
+        }
+        __syncthreads();
         CollideParams cp;
-        cp.omega = 1.0 / dom.tau;
-        cp.inv_2tp = 1.0 / (2.0 * dom.tau);
-        cp.inv_2tm = 1.0 / (2.0 * dom.tau_minus);
-        cp.beta = 1.0 / (2.0 * dom.tau);
+        cp.omega = s_rates[0];
+        cp.inv_2tp = s_rates[1];
+        cp.inv_2tm = s_rates[2];
+        cp.beta = s_rates[1];
         const T *__restrict__ fin = pool_in + dom.offset;
         T *fout = pool_out + dom.offset;
         // a thread's cells advance by blockDim along the tile's rows: the
