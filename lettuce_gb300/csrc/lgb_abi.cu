@@ -696,6 +696,7 @@ int lgb_step(const lgb_step_desc *d, void *stream) {
     p.cp.inv_2tp = 1.0 / (2.0 * d->tau);
     p.cp.inv_2tm = d->collision == LGB_TRT ? 1.0 / (2.0 * d->tau_minus) : 0.0;
     p.cp.beta = 1.0 / (2.0 * d->tau);
+    lgb::set_float_rates(p.cp);
     p.cp.tau = d->tau;
     p.cp.smag_c2 = d->smagorinsky_constant * d->smagorinsky_constant;
     p.mrt_host = d->mrt_tables;

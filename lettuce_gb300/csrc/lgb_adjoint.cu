@@ -121,6 +121,7 @@ extern "C" int lgb_adjoint_step(int32_t stencil, int32_t storage, const int32_t 
     p.divZ = lgb::FastDiv::make(p.Z);
     p.divY = lgb::FastDiv::make(p.Y);
     p.cp.omega = 1.0 / tau;
+    lgb::set_float_rates(p.cp);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaErrorInvalidValue;
     switch (stencil) {

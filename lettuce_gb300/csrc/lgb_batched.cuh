@@ -150,6 +150,7 @@ batched_step_kernel(const BatchParams p) {
         cp.inv_2tp = s_rates[1];
         cp.inv_2tm = s_rates[2];
         cp.beta = s_rates[1];
+        set_float_rates(cp);
         const T *__restrict__ fin = pool_in + dom.offset;
         T *fout = pool_out + dom.offset;
         // a thread's cells advance by blockDim along the tile's rows: the

@@ -90,7 +90,21 @@ struct CollideParams {
     double src_scale;    // Guo: 1 - 1 / (2 tau_force); otherwise 0
     double tau;          // Smagorinsky: the molecular relaxation time
     double smag_c2;      // Smagorinsky constant squared
+    // the float32 rates of the shifted-space BGK / TRT (lgb_shifted.cuh),
+    // rounded once on the host by set_float_rates: (float) omega,
+    // (float) (1 - omega), (float) inv_2tp, (float) inv_2tm. Formed per
+    // thread from the doubles above they occupied the float64 pipe a fifth
+    // of the 16-bit pull launch.
+    float f_omega, f_one_minus_omega, f_inv_2tp, f_inv_2tm;
 };
+
+// fill the float32 copies of the rates from the float64 ones
+LGB_HD void set_float_rates(CollideParams &cp) {
+    cp.f_omega = (float)cp.omega;
+    cp.f_one_minus_omega = (float)(1.0 - cp.omega);
+    cp.f_inv_2tp = (float)cp.inv_2tp;
+    cp.f_inv_2tm = (float)cp.inv_2tm;
+}
 
 template <class S, class R>
 LGB_HD void collide_bgk(R (&f)[S::Q], const CollideParams &cp, R &rho_out) {

@@ -109,8 +109,8 @@ __device__ __forceinline__ void collide_shifted(typename L::V (&h)[S::Q], const 
         const V k45 = L::mul(inv, L::set(4.5f));
         if constexpr (COLL == LGB_BGK) {
             // h' = (1 - omega) h + (omega w_q) X_q
-            const float om = (float)cp.omega;
-            const V om1 = L::set((float)(1.0 - cp.omega));
+            const float om = cp.f_omega;
+            const V om1 = L::set(cp.f_one_minus_omega);
             h[0] = L::fma(L::set(om * (float)S::w(0)), base, L::mul(om1, h[0]));
 #pragma unroll
             for (int q = 1; q < S::Q; ++q) {
@@ -127,8 +127,8 @@ __device__ __forceinline__ void collide_shifted(typename L::V (&h)[S::Q], const 
             //   dp = (h_q + h_o) - 2 w s,  dm = (h_q - h_o) - 6 w ej,
             //   h_q' = h_q - dp / (2 tau+) - dm / (2 tau-),
             //   h_o' = h_o - dp / (2 tau+) + dm / (2 tau-)
-            const V nap = L::set((float)-cp.inv_2tp);
-            const V am = L::set((float)cp.inv_2tm), nam = L::set((float)-cp.inv_2tm);
+            const V nap = L::set(-cp.f_inv_2tp);
+            const V am = L::set(cp.f_inv_2tm), nam = L::set(-cp.f_inv_2tm);
             {
                 const V dp = L::fma(L::set(-2.0f * (float)S::w(0)), base, L::add(h[0], h[0]));
                 h[0] = L::fma(nap, dp, h[0]);

@@ -58,6 +58,7 @@ unsigned long long run(int coll, double tau, double tau_minus, int pairs, unsign
     cp.inv_2tp = 1.0 / (2.0 * tau);
     cp.inv_2tm = 1.0 / (2.0 * tau_minus);
     cp.beta = 1.0 / (2.0 * tau);
+    set_float_rates(cp);
     const int blocks = (pairs + 255) / 256;
     if (coll == LGB_BGK) compare<S, LGB_BGK><<<blocks, 256>>>(d, pairs, cp, bad);
     else compare<S, LGB_TRT><<<blocks, 256>>>(d, pairs, cp, bad);
