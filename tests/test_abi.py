@@ -182,3 +182,43 @@ def test_batch_struct_layouts_match_header(tmp_path, lgb):
     assert got == [DOMAIN_DTYPE.itemsize, DOMAIN_DTYPE.fields["tau"][1], TILE_DTYPE.itemsize,
                    ctypes.sizeof(BatchDesc), BatchDesc.domains.offset, BatchDesc.f_out.offset,
                    BatchDesc.pool_elements.offset, BatchDesc.status.offset]
+
+
+def test_init_and_enstrophy_validation(lgb):
+    """lgb_equilibrium, lgb_init_fneq and lgb_enstrophy refuse bad arguments
+    before any device call"""
+    from lettuce_gb300 import _lib
+    L = _lib.load()
+    r2 = _lib.i32x3([8, 6])
+    rs = (ctypes.c_int64 * 3)(0, 0, 0)
+    us = (ctypes.c_int64 * 4)(0, 0, 0, 0)
+    R, RS, US = (ctypes.cast(x, ctypes.c_void_p) for x in (r2, rs, us))
+    cases = [
+        (lambda: L.lgb_equilibrium(9, _lib.F32, R, 0x1000, RS, 0x2000, US, 0x3000, None, None,
+                                   None), "unknown stencil"),
+        (lambda: L.lgb_equilibrium(_lib.D2Q9, 7, R, 0x1000, RS, 0x2000, US, 0x3000, None, None,
+                                   None), "unknown storage"),
+        (lambda: L.lgb_equilibrium(_lib.D2Q9, _lib.F32, R, None, RS, 0x2000, US, 0x3000, None,
+                                   None, None), "NULL"),
+        (lambda: L.lgb_equilibrium(_lib.D2Q9, _lib.F32, R, 0x1000, RS, 0x2000, US, None, None,
+                                   None, None), "neither"),
+        (lambda: L.lgb_equilibrium(_lib.D2Q9, _lib.F32, R, 0x1000, RS, 0x2000, US, None, 0x4000,
+                                   None, None), "go together"),
+        (lambda: L.lgb_init_fneq(_lib.D2Q9, _lib.F32, R, 0x1000, 0x2000, 0.0, 0x3000, None),
+         "tau must be positive"),
+        (lambda: L.lgb_init_fneq(_lib.D1Q3, _lib.F32, R, 0x1000, 0x2000, 0.6, 0x3000, None),
+         "2-D or 3-D"),
+        (lambda: L.lgb_init_fneq(_lib.D2Q9, _lib.F32, R, 0x1000, None, 0.6, 0x3000, None),
+         "NULL"),
+        (lambda: L.lgb_enstrophy(4, _lib.F32, R, 0x1000, 0x2000, 0x3000, None), "dimensions"),
+        (lambda: L.lgb_enstrophy(2, _lib.F16_SHIFTED, R, 0x1000, 0x2000, 0x3000, None),
+         "precision"),
+        (lambda: L.lgb_enstrophy(2, _lib.F32, R, 0x1000, 0x2000, None, None), "NULL"),
+    ]
+    for call, msg in cases:
+        assert call() != 0
+        assert msg in L.lgb_last_error().decode(), (msg, L.lgb_last_error())
+    bad = _lib.i32x3([0, 6])
+    assert L.lgb_enstrophy(2, _lib.F64, ctypes.cast(bad, ctypes.c_void_p), 0x1000, 0x2000,
+                           0x3000, None) != 0
+    assert "must be positive" in L.lgb_last_error().decode()
