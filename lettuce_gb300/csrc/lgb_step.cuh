@@ -115,49 +115,41 @@ __device__ __forceinline__ void load_cell(const StepParams &p, const typename St
                                           const Nbr &c, uint32_t n, uint32_t nsbits,
                                           typename Sto::R (&f)[S::Q], uint32_t lbits = 0) {
     const size_t N = p.N;
-    using T = typename Sto::T;
-#pragma unroll
-    for (int q = 0; q < S::Q; ++q) {
-        uint32_t src = n;
-        int slot = q;
-        if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
-            src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
-            if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
-        }
-        const T *ptr = fin + (size_t)slot * N + src;
-        if constexpr (RAW) f[q] = Sto::load_h(ptr);
-        else f[q] = Sto::load(ptr, S::w(q));
-    }
-    // A pull with no-streaming bits keeps the cell's own value for those
+    // a pull with no-streaming bits keeps the cell's own value for those
     // populations, and a halfway bounce-back link takes the cell's own
-    // opposite population: those few cells load the kept values again over
-    // the pulled ones. The pulled loads above do not wait for the cell's
-    // flag and bit words (every pulled address is inside the periodic
-    // grid), so for nearly all cells they overlap the flag load instead of
-    // following it.
-    if constexpr (MASKED && LOAD == LOAD_PULL) {
-        if ((nsbits | (LINKS ? lbits : 0u)) != 0) {
+    // opposite population; cells without either (nearly all) skip the
+    // per-population test
+    const bool keep_own = MASKED && LOAD == LOAD_PULL && (nsbits | (LINKS ? lbits : 0u)) != 0;
+    using T = typename Sto::T;
+    auto load_all = [&](const bool check) {
 #pragma unroll
-            for (int q = 1; q < S::Q; ++q) {
+        for (int q = 0; q < S::Q; ++q) {
+            uint32_t src = n;
+            int slot = q;
+            if (LOAD == LOAD_PULL || LOAD == LOAD_AA_ODD) {
+                src = c.at(-ix<S>(q), -iy<S>(q), -iz<S>(q), p);
+                if (LOAD == LOAD_AA_ODD) slot = S::opp(q);
+            }
+            const T *ptr = fin + (size_t)slot * N + src;
+            if (LOAD == LOAD_PULL && check && q != 0) {
                 // the bounce follows the stream (halfway_bounce_back_boundary.py:
                 // 182-190 runs after ebb_simulation.py:76), so a link wins
                 // over a no-streaming bit. A halfway link takes the cell's own
                 // post-collision opp(q); an interpolated one the value the
                 // link pass stored (same storage format)
-                const T *ptr = nullptr;
                 if (LINKS && ((lbits >> q) & 1u))
                     ptr = p.link_val ? static_cast<const T *>(p.link_val) + p.link_base[n] +
                                            __popc(lbits & ((1u << q) - 1u))
                                      : fin + (size_t)S::opp(q) * N + n;
                 else if ((nsbits >> q) & 1u)
                     ptr = fin + (size_t)q * N + n;
-                if (ptr) {
-                    if constexpr (RAW) f[q] = Sto::load_h(ptr);
-                    else f[q] = Sto::load(ptr, S::w(q));
-                }
             }
+            if constexpr (RAW) f[q] = Sto::load_h(ptr);
+            else f[q] = Sto::load(ptr, S::w(q));
         }
-    }
+    };
+    if (keep_own) load_all(true);
+    else load_all(false);
 }
 
 // the substep with index `idx`, copied out of the parameter block by an
