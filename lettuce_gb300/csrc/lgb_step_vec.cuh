@@ -157,14 +157,22 @@ __device__ __forceinline__ void step_pair(const StepParams &p, const uint32_t t,
 #ifndef LGB_VEC2_2D_MIN_BLOCKS
 #define LGB_VEC2_2D_MIN_BLOCKS 6
 #endif
-template <int SID>
+// the scattering patterns (PUSH, AA_ODD) of D3Q15 / D3Q19 keep the shuffled
+// pair words of the stores live as well; 0 = the bound of their stencil
+#ifndef LGB_VEC2_SCATTER_MIN_BLOCKS
+#define LGB_VEC2_SCATTER_MIN_BLOCKS 0
+#endif
+template <int SID, int PAT>
 constexpr int vec2_min_blocks() {
     return SID == LGB_D3Q27 ? LGB_VEC2_D3Q27_MIN_BLOCKS
-                            : ((SID == LGB_D2Q9 || SID == LGB_D1Q3) ? LGB_VEC2_2D_MIN_BLOCKS
-                                                                  : LGB_VEC2_MIN_BLOCKS);
+           : (SID == LGB_D2Q9 || SID == LGB_D1Q3)
+               ? LGB_VEC2_2D_MIN_BLOCKS
+               : ((LGB_VEC2_SCATTER_MIN_BLOCKS > 0 && (PAT == LGB_PUSH || PAT == LGB_AA_ODD))
+                      ? LGB_VEC2_SCATTER_MIN_BLOCKS
+                      : LGB_VEC2_MIN_BLOCKS);
 }
 template <int SID, int ST, int COLL, int PAT>
-__global__ void __launch_bounds__(256, vec2_min_blocks<SID>())
+__global__ void __launch_bounds__(256, (vec2_min_blocks<SID, PAT>()))
 step_vec2_kernel(const StepParams p) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Nh = p.N >> 1;
