@@ -19,12 +19,6 @@
 
 #include "lgb_stencil.cuh"
 
-// the float32 KBC over opposite pairs in packed f32x2 arithmetic (1) or in
-// scalar arithmetic (0)
-#ifndef LGB_KBC_PACKED
-#define LGB_KBC_PACKED 1
-#endif
-
 namespace lgb {
 
 template <class S, class R>
@@ -335,47 +329,17 @@ LGB_HD void collide_kbc_of(const P &f, const CollideParams &cp, R &rho_out) {
         sum_s = d_s * dh * ifeq;
         sum_h = dh * dh * ifeq;
     }
-#if defined(__CUDA_ARCH__) && LGB_KBC_PACKED
-    // float32: each opposite pair (q, o) as one float2, the lanes of the
-    // packed f32x2 instructions (the pair's equilibrium, delta_h, the
-    // entropic sums, which each lane accumulates apart, and the update)
-    constexpr bool PACKED = sizeof(R) == 4;
-#else
-    constexpr bool PACKED = false;
-#endif
-    if constexpr (PACKED) {
-#if defined(__CUDA_ARCH__)
-        float2 ss = make_float2(0.0f, 0.0f), sh = make_float2(0.0f, 0.0f);
 #pragma unroll
-        for (int q = 1; q < S::Q; ++q) {
-            const int o = S::opp(q);
-            if (o < q) continue;
-            R fq, fo;
-            feq_pair(q, fq, fo);
-            const R d_s = ds(q);
-            const float2 nfe = make_float2(-fq, -fo);
-            const float2 h = __fadd2_rn(__fadd2_rn(make_float2(f.get(q), f.get(o)), nfe),
-                                        make_float2(-d_s, -d_s));
-            const float2 hi = __fmul2_rn(h, make_float2(kbc_rcp(fq), kbc_rcp(fo)));
-            ss = __ffma2_rn(make_float2(d_s, d_s), hi, ss);
-            sh = __ffma2_rn(h, hi, sh);
-        }
-        sum_s += ss.x + ss.y;
-        sum_h += sh.x + sh.y;
-#endif
-    } else {
-#pragma unroll
-        for (int q = 1; q < S::Q; ++q) {
-            const int o = S::opp(q);
-            if (o < q) continue;
-            R fq, fo;
-            feq_pair(q, fq, fo);
-            const R d_s = ds(q);
-            const R hq = f.get(q) - fq - d_s, ho = f.get(o) - fo - d_s;
-            const R iq = kbc_rcp(fq), io = kbc_rcp(fo);
-            sum_s += d_s * (hq * iq + ho * io);
-            sum_h += hq * hq * iq + ho * ho * io;
-        }
+    for (int q = 1; q < S::Q; ++q) {
+        const int o = S::opp(q);
+        if (o < q) continue;
+        R fq, fo;
+        feq_pair(q, fq, fo);
+        const R d_s = ds(q);
+        const R hq = f.get(q) - fq - d_s, ho = f.get(o) - fo - d_s;
+        const R iq = kbc_rcp(fq), io = kbc_rcp(fo);
+        sum_s += d_s * (hq * iq + ho * io);
+        sum_h += hq * hq * iq + ho * ho * io;
     }
     const R beta = R(cp.beta);
     const R ib = R(1) / beta;
@@ -388,39 +352,17 @@ LGB_HD void collide_kbc_of(const P &f, const CollideParams &cp, R &rho_out) {
         const R f0 = f.get(0);
         f.set(0, f0 - b2 * d_s - bg * (f0 - feq0 - d_s));
     }
-    if constexpr (PACKED) {
-#if defined(__CUDA_ARCH__)
-        // f' = (f - b2 d_s) - bg (f - feq - d_s)
-        const float2 nbg = make_float2(-bg, -bg);
 #pragma unroll
-        for (int q = 1; q < S::Q; ++q) {
-            const int o = S::opp(q);
-            if (o < q) continue;
-            R fq, fo;
-            feq_pair(q, fq, fo);
-            const R d_s = ds(q);
-            const float2 g = make_float2(f.get(q), f.get(o));
-            const float2 h = __fadd2_rn(__fadd2_rn(g, make_float2(-fq, -fo)),
-                                        make_float2(-d_s, -d_s));
-            const R nb2 = -(b2 * d_s);
-            const float2 out = __ffma2_rn(nbg, h, __fadd2_rn(g, make_float2(nb2, nb2)));
-            f.set(q, out.x);
-            f.set(o, out.y);
-        }
-#endif
-    } else {
-#pragma unroll
-        for (int q = 1; q < S::Q; ++q) {
-            const int o = S::opp(q);
-            if (o < q) continue;
-            R fq, fo;
-            feq_pair(q, fq, fo);
-            const R d_s = ds(q);
-            const R gq = f.get(q), go = f.get(o);
-            const R hq = gq - fq - d_s, ho = go - fo - d_s;
-            f.set(q, gq - b2 * d_s - bg * hq);
-            f.set(o, go - b2 * d_s - bg * ho);
-        }
+    for (int q = 1; q < S::Q; ++q) {
+        const int o = S::opp(q);
+        if (o < q) continue;
+        R fq, fo;
+        feq_pair(q, fq, fo);
+        const R d_s = ds(q);
+        const R gq = f.get(q), go = f.get(o);
+        const R hq = gq - fq - d_s, ho = go - fo - d_s;
+        f.set(q, gq - b2 * d_s - bg * hq);
+        f.set(o, go - b2 * d_s - bg * ho);
     }
     rho_out = rho;
 }
