@@ -39,6 +39,13 @@ template <> struct Pack16<LGB_BF16_SHIFTED> {
     }
 };
 
+// PUSH / AA_ODD stores of a shifted pair: 16-bit halves at the shifted
+// cells (1) or whole words composed through lane shuffles, with halves only
+// at row ends and warp edges (0)
+#ifndef LGB_VEC2_HALF_STORES
+#define LGB_VEC2_HALF_STORES 0
+#endif
+
 // the pair (z0 + dz, z0 + 1 + dz) of a row, dz in {-1, 0, 1}, from the
 // aligned words at pair index tz and its periodic neighbours
 __device__ __forceinline__ uint32_t load_pair(const uint32_t *__restrict__ row, uint32_t tz,
@@ -106,6 +113,15 @@ __device__ __forceinline__ void step_pair_at(const StepParams &p, const uint32_t
             const int dz = iz<S>(q);
             if (dz == 0) {
                 r[tz] = w;
+            } else if constexpr (LGB_VEC2_HALF_STORES) {
+                // each cell's value stored as its own 16-bit half at the
+                // shifted cell (the two halves of a destination word come
+                // from neighbouring lanes and meet in L2)
+                unsigned short *r16 = reinterpret_cast<unsigned short *>(r);
+                const uint32_t lo_dst = dz > 0 ? 2 * tz + 1 : (tz == 0 ? p.Z - 1 : 2 * tz - 1);
+                const uint32_t hi_dst = dz > 0 ? (tz + 1 == Zh ? 0 : 2 * tz + 2) : 2 * tz;
+                r16[lo_dst] = (unsigned short)(w & 0xffffu);
+                r16[hi_dst] = (unsigned short)(w >> 16);
             } else {
                 // the shifted pair straddles two words. A word whose two
                 // halves come from pairs held by neighbouring lanes of one
