@@ -13,10 +13,12 @@ family (D3Q27 KBC obstacle, also over its full 5000 steps with the sphere's
 drag, 256 batched D2Q9 domains, the D2Q9 adjoint); ``--no-configs`` skips
 them.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference|lettuce]
 
 ``--impl reference`` times the CPU oracle (a C restatement of lettuce's torch
-step) on this host's cores instead.
+step) on this host's cores instead; ``--impl lettuce`` times lettuce itself
+(installed in baseline/_ref): its generated cuda_native kernel and its torch
+path on the GPU, and its torch path on the host cores.
 """
 from __future__ import annotations
 
@@ -225,6 +227,171 @@ def run_reference(args, world, rank):
                 "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def import_lettuce():
+    """lettuce itself from its offline install in baseline/_ref (``pip install
+    --target``), its optional file-output imports (h5py, mmh3, pyevtk,
+    matplotlib) from the stand-ins in tests/golden/_stubs: (module, None) or
+    (None, why)"""
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isfile(os.path.join(ref, "lettuce", "__init__.py")):
+        return None, "lettuce is not installed in baseline/_ref"
+    for p in (os.path.join(ROOT, "tests", "golden", "_stubs"), ref):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    import warnings
+    try:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            import lettuce
+    except Exception as e:  # noqa: BLE001 - reported, not raised
+        return None, f"import lettuce failed: {type(e).__name__}: {e}"
+    return lettuce, None
+
+
+def run_lettuce(args, world, rank):
+    """lettuce's own paths for the headline workload (D3Q19 BGK Taylor-Green,
+    float32, PRE_STREAMING), timed for comparison: its generated cuda_native
+    kernel (lettuce/cuda_native, built at run time by lettuce's Generator
+    with nvcc) and its torch path on the GPU at 256^3, each through
+    ``Simulation.__call__`` between CUDA events; its torch path on the host
+    cores on a bounded sample; and how far lettuce's cuda_native field lies
+    from this package's after 10 steps from the same 32^3 initial field."""
+    if rank != 0:
+        return 0
+    import contextlib
+    import torch
+    L, why = import_lettuce()
+    line = {"impl": "lettuce", "metric": METRIC, "unit": UNIT, "dtype": "f32",
+            "config": {"workload": WORKLOAD, "grid": RES, "strategy": "PRE_STREAMING"}}
+    if L is None:
+        line["unavailable"] = why
+        print(json.dumps(line), flush=True)
+        return 0
+    try:
+        from importlib import metadata
+        version = metadata.version("lettuce")
+    except Exception:  # noqa: BLE001 - a name only
+        version = getattr(L, "__version__", None)
+    line["lettuce"] = {"version": version, "from": "baseline/_ref"}
+    S = L.StreamingStrategy.PRE_STREAMING
+
+    how = {}
+
+    def simulation(flow):
+        import io
+        import re
+        out = io.StringIO()
+        try:
+            with contextlib.redirect_stdout(out):
+                return L.Simulation(flow, L.BGKCollision(flow.units.relaxation_parameter_lu),
+                                    [], streaming_strategy=S)
+        except subprocess.CalledProcessError:
+            # lettuce's Generator wrote its sources and ran `setup.py install`
+            # there, which failed: build the same sources with the same
+            # setup.py in place, put the folder on sys.path, and let lettuce's
+            # own resolve step import the module on the next construction
+            sys.stderr.write(out.getvalue())
+            m = re.search(r"Installing Native module \((.*?)\)", out.getvalue())
+            if m is None:
+                raise
+            folder = m.group(1)
+            try:
+                tail = open(os.path.join(folder, "install.log")).read().strip().splitlines()[-3:]
+            except OSError:
+                tail = []
+            how["install_failed"] = " | ".join(x.strip() for x in tail)[-400:]
+            with open(os.path.join(folder, "build_ext.log"), "wb") as log:
+                rc = subprocess.run([sys.executable, "setup.py", "build_ext", "--inplace"],
+                                    cwd=folder, stdout=log, stderr=log).returncode
+            if rc != 0:
+                tail = open(os.path.join(folder, "build_ext.log")).read().strip().splitlines()
+                raise RuntimeError("lettuce's generated module did not build: "
+                                   + " | ".join(tail[-3:]))
+            how["built_by"] = "setup.py build_ext --inplace in lettuce's generated folder"
+            sys.path.insert(0, folder)
+            with contextlib.redirect_stdout(sys.stderr):
+                return L.Simulation(flow, L.BGKCollision(flow.units.relaxation_parameter_lu),
+                                    [], streaming_strategy=S)
+        finally:
+            sys.stderr.write(out.getvalue())
+
+    def build(device, use_native, res):
+        ctx = L.Context(device=device, dtype=torch.float32, use_native=use_native)
+        flow = L.TaylorGreenVortex(ctx, list(res), RE, MA, L.D3Q19())
+        sim = simulation(flow)
+        native = getattr(sim._collide_and_stream, "__module__", "") or ""
+        return flow, sim, native.startswith("lettuce_")
+
+    def gpu_leg(use_native):
+        dev = torch.device("cuda:0")
+        t0 = time.perf_counter()
+        flow, sim, is_native = build(dev, use_native, RES)
+        setup_s = time.perf_counter() - t0
+        if use_native and not is_native:
+            return {"unavailable": "lettuce's Generator did not install its cuda_native "
+                                   "module (see stderr)", "setup_s": round(setup_s, 1)}
+        with contextlib.redirect_stdout(sys.stderr):
+            sim(args.warmup)
+        torch.cuda.synchronize(dev)
+        stream = torch.cuda.current_stream(dev)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        ret = sim(args.steps)
+        end.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = start.elapsed_time(end) / args.steps
+        n = int(np.prod(RES))
+        out = {"mlups": round(n / ms / 1e3, 1), "ms_per_step": round(ms, 4),
+               "achieved_gbs": round(n * BYTES_PER_CELL["f32"] / ms / 1e6, 1),
+               "lettuce_return_mlups": round(float(ret), 1), "setup_s": round(setup_s, 1)}
+        del flow, sim
+        torch.cuda.empty_cache()
+        return out
+
+    if torch.cuda.is_available():
+        peak, _ = peaks()
+        line["cuda_native"] = gpu_leg(True)
+        line["cuda_native"].update(how)
+        line["torch_gpu"] = gpu_leg(False)
+        for leg in ("cuda_native", "torch_gpu"):
+            if "achieved_gbs" in line[leg]:
+                line[leg]["frac_of_peak"] = round(line[leg]["achieved_gbs"] / peak, 4)
+        if "mlups" in line["cuda_native"]:
+            # lettuce's generated kernel against this package's from one initial field
+            import lettuce_gb300 as lt
+            flow, sim, _ = build(torch.device("cuda:0"), True, [32, 32, 32])
+            f0 = flow.f.detach().cpu().clone()
+            with contextlib.redirect_stdout(sys.stderr):
+                sim(10)
+            got = flow.f.detach().cpu().double()
+            ours_flow = lt.TaylorGreenVortex(lt.Context("cuda:0", torch.float32),
+                                             [32, 32, 32], RE, MA, lt.D3Q19)
+            ours_flow.f = f0.to("cuda:0")
+            ours = lt.Simulation(ours_flow, lt.BGKCollision(ours_flow.units.relaxation_parameter_lu),
+                                 [], streaming_strategy=lt.StreamingStrategy.PRE_STREAMING)
+            ours(10)
+            mine = ours_flow.f.detach().cpu().double()
+            line["cuda_native"]["max_rel_diff_vs_lettuce_gb300_32cube_10_steps"] = float(
+                ((got - mine).abs().max() / mine.abs().max()).item())
+    # lettuce's torch path on the host cores, bounded sample
+    nthreads = os.cpu_count() or 1
+    torch.set_num_threads(nthreads)
+    cpu_res = [int(x) for x in os.environ.get("LGB_LETTUCE_CPU_GRID", "256,256,256").split(",")]
+    flow, sim, _ = build("cpu", False, cpu_res)
+    sim(1)
+    t0 = time.perf_counter()
+    ret = sim(2)
+    dt = time.perf_counter() - t0
+    line["torch_cpu"] = {"mlups": round(2 * int(np.prod(cpu_res)) / dt / 1e6, 3),
+                         "lettuce_return_mlups": round(float(ret), 3), "cores": nthreads,
+                         "sample": f"2 steps on {cpu_res[0]}x{cpu_res[1]}x{cpu_res[2]} after one "
+                                   f"warm-up step, torch {torch.__version__}, "
+                                   f"{nthreads} intra-op threads"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -880,7 +1047,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
-    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--impl", choices=["ours", "reference", "lettuce"], default="ours",
+                    help="reference: the CPU oracle on the host cores; lettuce: lettuce "
+                         "itself from baseline/_ref (its cuda_native and torch paths)")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -907,6 +1076,8 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args, world, rank)
+        if args.impl == "lettuce":
+            return run_lettuce(args, world, rank)
         return run_ours(args, world, rank, local)
     finally:
         if world > 1:

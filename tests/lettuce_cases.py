@@ -11,7 +11,34 @@ KBC, regularized, Smagorinsky, MRT (Dellar), no collision; bounce-back,
 equilibrium inlet, anti-bounce-back and pressure outlets, partially
 saturated cells; a pre-collision boundary (lettuce's collision index 1, whose
 no-streaming mask starts at 1 everywhere)."""
+import os
+import sys
+
 import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_lettuce():
+    """lettuce itself, or None: from ``$LETTUCE_SRC`` (its source folder) or
+    from its offline install in ``baseline/_ref`` (``pip install --target``),
+    its optional file-output imports from the stand-ins in
+    ``tests/golden/_stubs``"""
+    root = os.path.dirname(HERE)
+    for src in (os.environ.get("LETTUCE_SRC"), os.path.join(root, "baseline", "_ref")):
+        if src and os.path.isfile(os.path.join(src, "lettuce", "__init__.py")):
+            for p in (os.path.join(HERE, "golden", "_stubs"), src):
+                if p not in sys.path:
+                    sys.path.insert(0, p)
+            break
+    import warnings
+    try:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            import lettuce
+    except ImportError:
+        return None
+    return lettuce if hasattr(lettuce, "Simulation") else None
 
 
 def _sphere(res, centre, radius):

@@ -8,11 +8,11 @@ pointers zeroed, the launch patterns, the flag byte and no-streaming word
 packed from lettuce's own masks, the inlet and MRT tables. The simulations
 of ``tests/lettuce_cases.py`` built from this package's mirror classes must
 give the same, and the mirror's own ``Simulation`` descriptor must agree with
-the binding's. With lettuce importable (its source folder on ``sys.path`` or
-in ``$LETTUCE_SRC``, the stand-ins of ``tests/golden/_stubs`` for its
-optional imports) the binding is also run on lettuce's objects directly."""
+the binding's. With lettuce importable (its source folder in
+``$LETTUCE_SRC`` or its install in ``baseline/_ref``, the stand-ins of
+``tests/golden/_stubs`` for its optional imports) the binding is also run on
+lettuce's objects directly."""
 import os
-import sys
 
 import numpy as np
 import pytest
@@ -20,7 +20,7 @@ import torch
 
 import lettuce_gb300 as lt
 from conftest import GOLDEN
-from lettuce_cases import cases, desc_signature, step_record
+from lettuce_cases import cases, desc_signature, import_lettuce, step_record
 
 DTYPES = {"f64": torch.float64, "f32": torch.float32}
 
@@ -61,16 +61,10 @@ def test_mirror_builds_lettuces_descriptors(tag):
 
 
 def _import_lettuce():
-    src = os.environ.get("LETTUCE_SRC")
-    if src and src not in sys.path:
-        sys.path.insert(0, src)
-        sys.path.insert(0, os.path.join(GOLDEN, "_stubs"))
-    try:
-        import lettuce
-    except ImportError:
-        pytest.skip("lettuce is not importable (set LETTUCE_SRC to its source folder)")
-    if not hasattr(lettuce, "Simulation"):
-        pytest.skip("an unrelated 'lettuce' module is on the path")
+    lettuce = import_lettuce()
+    if lettuce is None:
+        pytest.skip("lettuce is not importable (set LETTUCE_SRC to its source folder "
+                    "or install it in baseline/_ref)")
     return lettuce
 
 
