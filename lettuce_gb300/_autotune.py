@@ -1,6 +1,7 @@
 """Launch-shape tuner of the batched step, with an on-disk cache.
 
-Candidates: threads per block x tile size (cells per tile). Each candidate
+Candidates: threads per block x tile size (cells per tile) x grid (persistent
+blocks walking the tile table, or one block per tile). Each candidate
 is timed with CUDA events over a few steps of the actual batch (the pools
 are saved before and restored after, so tuning does not advance the
 simulation). The fastest is stored under a key made of the device name,
@@ -44,9 +45,10 @@ def lookup(sim):
     return _load().get(_key(sim))
 
 
-def time_config(sim, threads: int, tile_cells: int, steps: int = 10, warmup: int = 3) -> float:
+def time_config(sim, threads: int, tile_cells: int, persistent: bool = True, steps: int = 10,
+                warmup: int = 3) -> float:
     """milliseconds per step of one launch shape (eager launches)"""
-    sim._configure(threads, tile_cells)
+    sim._configure(threads, tile_cells, persistent)
     stream = torch.cuda.current_stream(sim.context.device)
     for _ in range(warmup):
         sim.step_once()
@@ -67,16 +69,18 @@ def tune(sim, save: bool = True) -> dict:
     try:
         for t in THREADS:
             for c in TILE_CELLS:
-                ms = time_config(sim, t, c)
-                results[f"{t}x{c}"] = ms
-                if best is None or ms < best[0]:
-                    best = (ms, t, c)
+                for pers in (True, False):
+                    ms = time_config(sim, t, c, pers)
+                    results[f"{t}x{c}{'' if pers else 'x1'}"] = ms
+                    if best is None or ms < best[0]:
+                        best = (ms, t, c, pers)
     finally:
         for p, s in zip(sim._pools, saved):
             p.copy_(s)
         sim._cur = cur
         torch.cuda.synchronize(sim.context.device)
-    cfg = {"threads": best[1], "tile_cells": best[2], "ms_per_step": best[0]}
+    cfg = {"threads": best[1], "tile_cells": best[2], "persistent": best[3],
+           "ms_per_step": best[0]}
     if save:
         data = _load()
         data[_key(sim)] = cfg

@@ -71,7 +71,8 @@ def plan_tiles(stencil_id: int, domains: np.ndarray, tile_cells: int) -> np.ndar
 
 class BatchedSimulation:
     def __init__(self, flows: Sequence, collisions: Sequence, tile_cells: Optional[int] = None,
-                 threads: Optional[int] = None, autotune: bool = True):
+                 threads: Optional[int] = None, autotune: bool = True,
+                 persistent: Optional[bool] = None):
         if len(flows) == 0 or len(flows) != len(collisions):
             raise ValueError("one collision per flow is required")
         f0 = flows[0]
@@ -150,17 +151,27 @@ class BatchedSimulation:
                 cfg = {"threads": 256, "tile_cells": 4096}
         self.threads = int(threads or cfg["threads"])
         self.tile_cells = int(tile_cells or cfg["tile_cells"])
-        self._configure(self.threads, self.tile_cells)
+        if persistent is None:
+            persistent = bool((cfg or {}).get("persistent", True))
+        self._configure(self.threads, self.tile_cells, persistent)
         self._bind_flows()
 
     # -- launch configuration ---------------------------------------------
-    def _configure(self, threads: int, tile_cells: int):
+    def _configure(self, threads: int, tile_cells: int, persistent: bool = True):
+        """launch shape: threads per block, cells per tile, and the grid --
+        persistent (as many blocks as the SMs hold, walking the tile table
+        with a grid stride) or one block per tile (the hardware's block
+        scheduler hands out the tiles)"""
         tiles = plan_tiles(self.stencil.lgb_id, self.domains, tile_cells)
         self.n_tiles = len(tiles)
         self._tiles_dev = torch.from_numpy(tiles.view(np.uint8).copy()).to(self.context.device)
         self.threads = threads
         self.tile_cells = tile_cells
-        self.blocks = max(1, min(self.n_tiles, self.sm_count * max(1, 2048 // threads)))
+        self.persistent = bool(persistent)
+        if self.persistent:
+            self.blocks = max(1, min(self.n_tiles, self.sm_count * max(1, 2048 // threads)))
+        else:
+            self.blocks = max(1, self.n_tiles)
         self._graph = None
 
     def _desc(self, src: torch.Tensor, dst: torch.Tensor) -> BatchDesc:
@@ -206,7 +217,7 @@ class BatchedSimulation:
             self._launch(self._pools[0], self._pools[1], st)
             self._launch(self._pools[1], self._pools[0], st)
         self._graph = _device.capture(self.context.device, pair)
-        self._graph_key = (self.threads, self.tile_cells)
+        self._graph_key = (self.threads, self.tile_cells, self.persistent)
 
     def advance(self, num_steps: int, use_graph: bool = True):
         """num_steps steps of every domain, asynchronous on the current stream"""
@@ -216,7 +227,8 @@ class BatchedSimulation:
             self.step_once()
             num_steps -= 1
         if use_graph and num_steps >= 2:
-            if self._graph is None or self._graph_key != (self.threads, self.tile_cells):
+            if self._graph is None or self._graph_key != (self.threads, self.tile_cells,
+                                                          self.persistent):
                 # the capture itself advances the pools by two steps
                 self._capture()
                 num_steps -= 2

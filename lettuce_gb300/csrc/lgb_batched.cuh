@@ -83,13 +83,98 @@ struct BatchParams {
     uint32_t *status;
 };
 
-// Registers: the compiler's choice (59-64 for the 16-bit D2Q9 batches).
-// Measured on the 256 config-4 domains, fp16: capped at 56 the same 136.3k
-// MLUPS, at 48 122.0k, at 40 104.2k -- the spills of a tighter cap cost more
-// than the occupancy it buys.
+// The 16-bit pair loop keeps its tile's domain in shared memory and reads
+// it there at every use (1), or holds it in registers (0). The kernel
+// parameters cost no registers (they are read from the constant bank), but
+// a tile's grid, word offset and rates do: in registers they lift the
+// D2Q9 kernel from the 42 registers of the single-grid two-cell kernel to
+// 62, and its occupancy from 75 % to 50 %.
+#ifndef LGB_BATCH_LEAN
+#define LGB_BATCH_LEAN 1
+#endif
+
+// a tile of a 16-bit domain as its pair loop reads it
+struct TilePairs {
+    uint64_t word_offset;  // the domain's first 32-bit word in the pool
+    uint32_t X, Y, Zh, Nh; // grid, words per row, words per population plane
+    uint32_t end;          // one past the tile's last pair (row Zh + word)
+    float f_omega, f_one_minus_omega, f_inv_2tp, f_inv_2tm;
+};
+
+// the pull step of the pairs t2, t2 + blockDim, ... below ts.end of a tile
+// (pair index = row Zh + word), the tile's values read from shared memory
+// where they are used; PADDED: the last word of a row holds (cell Z - 1,
+// pad), the pad lane is left out of the status check
+template <int SID, int ST, int COLL, bool PADDED>
+__device__ __forceinline__ void tile_pairs_pull(const BatchParams &p, const volatile TilePairs &ts,
+                                                uint32_t t2) {
+    using S = Stencil<SID>;
+    using P = Pack16<ST>;
+    uint32_t tz, x, y;
+    {
+        const uint32_t Zh = ts.Zh, Y = ts.Y;
+        const uint32_t row = t2 / Zh;
+        tz = t2 - row * Zh;
+        x = row / Y;
+        y = row - x * Y;
+    }
+    while (true) {
+        float2 h[S::Q];
+        {
+            const uint32_t X = ts.X, Y = ts.Y, Zh = ts.Zh, Nh = ts.Nh;
+            const uint32_t *__restrict__ fin =
+                static_cast<const uint32_t *>(p.f_in) + ts.word_offset;
+            const uint32_t xm = x == 0 ? X - 1 : x - 1, xp = x + 1 == X ? 0 : x + 1;
+            const uint32_t ym = y == 0 ? Y - 1 : y - 1, yp = y + 1 == Y ? 0 : y + 1;
+            const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) {
+                const int dx = -ix<S>(q), dy = -iy<S>(q);
+                const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
+                const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
+                const uint32_t *r = fin + (size_t)q * Nh + (a * Y + b) * Zh;
+                uint32_t w;
+                if constexpr (PADDED) w = load_pair_padded(r, tz, Zh, -iz<S>(q));
+                else w = load_pair(r, tz, tzm, tzp, -iz<S>(q));
+                h[q] = P::decode(w);
+            }
+        }
+        {
+            CollideParams cp;
+            cp.f_omega = ts.f_omega;
+            cp.f_one_minus_omega = ts.f_one_minus_omega;
+            cp.f_inv_2tp = ts.f_inv_2tp;
+            cp.f_inv_2tm = ts.f_inv_2tm;
+            collide_shifted<S, Lane2, COLL>(h, cp);
+        }
+        if (p.status) {
+            float2 r = h[0];
+#pragma unroll
+            for (int q = 1; q < S::Q; ++q) r = Lane2::add(r, h[q]);
+            if (!isfinite(r.x) || ((!PADDED || tz + 1 < ts.Zh) && !isfinite(r.y)))
+                atomicOr(p.status, 1u);
+        }
+        {
+            const uint32_t Nh = ts.Nh;
+            uint32_t *fout = static_cast<uint32_t *>(p.f_out) + ts.word_offset +
+                             (x * ts.Y + y) * ts.Zh + tz;
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) fout[(size_t)q * Nh] = P::encode(h[q]);
+        }
+        t2 += blockDim.x;
+        if (t2 >= ts.end) break;
+        const uint32_t Zh = ts.Zh;
+        tz += blockDim.x;
+        while (tz >= Zh) {
+            tz -= Zh;
+            if (++y == ts.Y) { y = 0; ++x; }
+        }
+    }
+}
+
+// the batched step (one launch over every tile of the batch)
 template <int SID, int ST, int COLL>
-__global__ void __launch_bounds__(512)
-batched_step_kernel(const BatchParams p) {
+__device__ __forceinline__ void batched_step_body(const BatchParams &p) {
     using S = Stencil<SID>;
     using Sto = Storage<ST>;
     using R = typename Sto::R;
@@ -98,6 +183,7 @@ batched_step_kernel(const BatchParams p) {
     const T *__restrict__ pool_in = static_cast<const T *>(p.f_in);
     T *pool_out = static_cast<T *>(p.f_out);
     __shared__ double s_rates[3];
+    __shared__ TilePairs s_pairs;
     for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
         const lgb_batch_tile tile = p.tiles[t];
         if (tile.domain < 0 || tile.domain >= p.n_domains) {
@@ -143,8 +229,37 @@ batched_step_kernel(const BatchParams p) {
             s_rates[0] = 1.0 / dom.tau;
             s_rates[1] = 1.0 / (2.0 * dom.tau);
             s_rates[2] = 1.0 / (2.0 * dom.tau_minus);
+            if constexpr (HSPACE && LGB_BATCH_LEAN) {
+                CollideParams c;
+                c.omega = s_rates[0];
+                c.inv_2tp = s_rates[1];
+                c.inv_2tm = s_rates[2];
+                set_float_rates(c);
+                s_pairs.f_omega = c.f_omega;
+                s_pairs.f_one_minus_omega = c.f_one_minus_omega;
+                s_pairs.f_inv_2tp = c.f_inv_2tp;
+                s_pairs.f_inv_2tm = c.f_inv_2tm;
+                s_pairs.word_offset = (uint64_t)dom.offset >> 1;
+                s_pairs.X = r[0];
+                s_pairs.Y = r[1];
+                s_pairs.Zh = pitch >> 1;
+                s_pairs.Nh = (uint32_t)(n_alloc >> 1);
+                s_pairs.end = (uint32_t)tile.row_end * (pitch >> 1);
+            }
         }
         __syncthreads();
+        if constexpr (HSPACE && LGB_BATCH_LEAN) {
+            // rows of whole 32-bit words: padded odd rows, or even rows at an
+            // even offset (the others are flagged and skipped below)
+            if (padded || ((r[2] & 1u) == 0 && (dom.offset & 1) == 0)) {
+                const uint32_t t2 = (uint32_t)tile.row_begin * (pitch >> 1) + threadIdx.x;
+                if (t2 < (uint32_t)tile.row_end * (pitch >> 1)) {
+                    if (padded) tile_pairs_pull<SID, ST, COLL, true>(p, s_pairs, t2);
+                    else tile_pairs_pull<SID, ST, COLL, false>(p, s_pairs, t2);
+                }
+                continue;
+            }
+        }
         CollideParams cp;
         cp.omega = s_rates[0];
         cp.inv_2tp = s_rates[1];
@@ -247,14 +362,53 @@ batched_step_kernel(const BatchParams p) {
     }
 }
 
+// Registers. The D2Q9 / D1Q3 batches of the 16-bit formats are capped at
+// LGB_BATCH_16BIT_2D_MAXREG, those of float32 at LGB_BATCH_F32_2D_MAXREG
+// (10 and 12 resident 128-thread blocks per SM instead of 8, no spills);
+// the other batches keep the compiler's choice. Measured on the 256
+// config-4 domains, fp16 TRT, best launch shape of each: the pair loop with
+// its tile in registers 132.9k MLUPS (62 registers); with its tile in shared
+// memory 126.1k (50), capped at 48 140.0k (no spills), at 44 136.6k (20
+// bytes of spills), at 40 134.8k (48 bytes).
+#ifndef LGB_BATCH_16BIT_2D_MAXREG
+#define LGB_BATCH_16BIT_2D_MAXREG 48
+#endif
+#ifndef LGB_BATCH_F32_2D_MAXREG
+#define LGB_BATCH_F32_2D_MAXREG 40
+#endif
+template <int SID, int ST>
+constexpr int batch_maxreg() {
+    return (SID != LGB_D2Q9 && SID != LGB_D1Q3) ? 0
+           : is_shifted<ST>()                    ? LGB_BATCH_16BIT_2D_MAXREG
+           : ST == LGB_F32                       ? LGB_BATCH_F32_2D_MAXREG
+                                                 : 0;
+}
+
+template <int SID, int ST, int COLL>
+__global__ void __launch_bounds__(512) batched_step_kernel(const BatchParams p) {
+    batched_step_body<SID, ST, COLL>(p);
+}
+
+template <int SID, int ST, int COLL>
+__global__ void __maxnreg__((batch_maxreg<SID, ST>() > 0 ? batch_maxreg<SID, ST>() : 64))
+batched_step_kernel_capped(const BatchParams p) {
+    batched_step_body<SID, ST, COLL>(p);
+}
+
+template <int SID, int ST, int COLL>
+void launch_batched_as(const BatchParams &p, int blocks, int threads, cudaStream_t s) {
+    if constexpr (batch_maxreg<SID, ST>() > 0)
+        batched_step_kernel_capped<SID, ST, COLL><<<blocks, threads, 0, s>>>(p);
+    else
+        batched_step_kernel<SID, ST, COLL><<<blocks, threads, 0, s>>>(p);
+}
+
 template <int SID, int ST>
 cudaError_t launch_batched(int coll, const BatchParams &p, int blocks, int threads, cudaStream_t s) {
     switch (coll) {
-    case LGB_NO_COLLISION:
-        batched_step_kernel<SID, ST, LGB_NO_COLLISION><<<blocks, threads, 0, s>>>(p);
-        break;
-    case LGB_BGK: batched_step_kernel<SID, ST, LGB_BGK><<<blocks, threads, 0, s>>>(p); break;
-    case LGB_TRT: batched_step_kernel<SID, ST, LGB_TRT><<<blocks, threads, 0, s>>>(p); break;
+    case LGB_NO_COLLISION: launch_batched_as<SID, ST, LGB_NO_COLLISION>(p, blocks, threads, s); break;
+    case LGB_BGK: launch_batched_as<SID, ST, LGB_BGK>(p, blocks, threads, s); break;
+    case LGB_TRT: launch_batched_as<SID, ST, LGB_TRT>(p, blocks, threads, s); break;
     default: return cudaErrorNotSupported;
     }
     return cudaGetLastError();

@@ -19,10 +19,12 @@ def _batch(storage=None, dtype=torch.float32, n=7, seed=3, lo=9, hi=70):
 @pytest.mark.parametrize("dtype,storage", [(torch.float64, None), (torch.float32, None),
                                            (torch.float32, "fp16_shifted"),
                                            (torch.float32, "bf16_shifted")])
-def test_batch_equals_single_domain_runs(lgb, dtype, storage):
+@pytest.mark.parametrize("persistent", [True, False], ids=["persistent", "block_per_tile"])
+def test_batch_equals_single_domain_runs(lgb, dtype, storage, persistent):
     flows, colls = _batch(storage, dtype)
     singles, scolls = _batch(storage, dtype)
-    sim = lt.BatchedSimulation(flows, colls, tile_cells=500, threads=128)
+    sim = lt.BatchedSimulation(flows, colls, tile_cells=500, threads=128, persistent=persistent)
+    assert sim.blocks == (min(sim.n_tiles, sim.sm_count * 16) if persistent else sim.n_tiles)
     sim(13)
     for fl, c, ref in zip(flows, scolls, singles):
         lt.Simulation(ref, c, [], lt.StreamingStrategy.PRE_STREAMING)(13)
@@ -70,7 +72,8 @@ def test_autotune_keeps_state_and_caches(lgb, tmp_path, monkeypatch):
         assert torch.equal(x.f_raw, y.f_raw)
     c, cc = _batch()
     sc = lt.BatchedSimulation(c, cc)          # cache hit: same shape, no retune
-    assert (sc.threads, sc.tile_cells) == (sa.threads, sa.tile_cells)
+    assert (sc.threads, sc.tile_cells, sc.persistent) == (sa.threads, sa.tile_cells,
+                                                          sa.persistent)
     assert not hasattr(sc, "tuning_results")
 
 
