@@ -2,8 +2,9 @@
 // persistent launch. All domains' population fields live in one pool (domain
 // b at element offset `offset`, layout [Q][N_b] as for a single grid); the
 // host cuts every domain into tiles of whole rows (lgb_batch_plan) and the
-// kernel's resident blocks walk the tile table with a grid stride, one cell
-// per thread, pulling from the periodic neighbours inside the tile's domain.
+// kernel's blocks walk the tile table with a grid stride (as many blocks as
+// the SMs hold, or one block per tile), one cell per thread, pulling from
+// the periodic neighbours inside the tile's domain.
 // The per-domain relaxation times come from the domain table. Domains of the
 // 16-bit formats whose rows are whole 32-bit words -- an even row length, or
 // an odd one stored with one pad element per row (pitch = length + 1) --
@@ -369,7 +370,9 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
 // config-4 domains, fp16 TRT, best launch shape of each: the pair loop with
 // its tile in registers 132.9k MLUPS (62 registers); with its tile in shared
 // memory 126.1k (50), capped at 48 140.0k (no spills), at 44 136.6k (20
-// bytes of spills), at 40 134.8k (48 bytes).
+// bytes of spills), at 40 134.8k (48 bytes); with the next pair's words
+// copied asynchronously (cp.async, 4 bytes each) into a two-stage
+// shared-memory buffer while the current pair collides, 110.8k.
 #ifndef LGB_BATCH_16BIT_2D_MAXREG
 #define LGB_BATCH_16BIT_2D_MAXREG 48
 #endif
