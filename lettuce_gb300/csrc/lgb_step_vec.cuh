@@ -63,24 +63,30 @@ __device__ __forceinline__ uint32_t load_pair(const uint32_t *__restrict__ row, 
 
 // the step of the cell pair tz (cells 2 tz, 2 tz + 1) of row (x, y) of the
 // grid p. For PUSH and AA_ODD, pair t = row Z/2 + tz must be held by lane
-// t mod 32 of a warp whose active lanes are `lanes`.
-template <int SID, int ST, int COLL, int PAT>
-__device__ __forceinline__ void step_pair_at(const StepParams &p, const uint32_t tz,
-                                             const uint32_t x, const uint32_t y,
-                                             const unsigned lanes = 0xffffffffu) {
+// t mod 32 of a warp whose active lanes are `lanes`. INTERIOR: the row's x
+// and y neighbours need no periodic wrap, so a neighbour row is the row
+// plus a fixed offset (the wrap along z is handled either way).
+template <int SID, int ST, int COLL, int PAT, bool INTERIOR>
+__device__ __forceinline__ void step_pair_body(const StepParams &p, const uint32_t tz,
+                                               const uint32_t x, const uint32_t y,
+                                               const unsigned lanes) {
     using S = Stencil<SID>;
     using P = Pack16<ST>;
     const uint32_t Zh = p.Z >> 1;
     const uint32_t Nh = p.N >> 1;
     const uint32_t row = x * p.Y + y;
-    const uint32_t xm = x == 0 ? p.X - 1 : x - 1, xp = x + 1 == p.X ? 0 : x + 1;
-    const uint32_t ym = y == 0 ? p.Y - 1 : y - 1, yp = y + 1 == p.Y ? 0 : y + 1;
     const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
     const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in);
     auto row_of = [&](int dx, int dy) -> uint32_t {
-        const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
-        const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
-        return (a * p.Y + b) * Zh;
+        if constexpr (INTERIOR) {
+            return row * Zh + (uint32_t)dx * (p.Y * Zh) + (uint32_t)dy * Zh;
+        } else {
+            const uint32_t xm = x == 0 ? p.X - 1 : x - 1, xp = x + 1 == p.X ? 0 : x + 1;
+            const uint32_t ym = y == 0 ? p.Y - 1 : y - 1, yp = y + 1 == p.Y ? 0 : y + 1;
+            const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
+            const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
+            return (a * p.Y + b) * Zh;
+        }
     };
 
     float2 h[S::Q];
@@ -154,6 +160,32 @@ __device__ __forceinline__ void step_pair_at(const StepParams &p, const uint32_t
             }
         }
     }
+}
+
+// Interior rows (no wrap along x or y) take the fixed-offset form; the
+// split is uniform over a warp whose pairs lie in one row. The shuffled
+// scatter stores (LGB_VEC2_HALF_STORES 0) need every lane of `lanes` in one
+// branch and keep the single form.
+#ifndef LGB_VEC2_INTERIOR
+#define LGB_VEC2_INTERIOR 1
+#endif
+template <int SID, int ST, int COLL, int PAT>
+__device__ __forceinline__ void step_pair_at(const StepParams &p, const uint32_t tz,
+                                             const uint32_t x, const uint32_t y,
+                                             const unsigned lanes = 0xffffffffu) {
+    using S = Stencil<SID>;
+    constexpr bool NBR = PAT == LGB_PULL || PAT == LGB_PUSH || PAT == LGB_AA_ODD;
+    constexpr bool SPLIT =
+        LGB_VEC2_INTERIOR && NBR && (LGB_VEC2_HALF_STORES || PAT == LGB_PULL);
+    if constexpr (SPLIT) {
+        const bool interior = (S::D < 3 || (x > 0 && x + 1 < p.X)) &&
+                              (S::D < 2 || (y > 0 && y + 1 < p.Y));
+        if (interior) {
+            step_pair_body<SID, ST, COLL, PAT, true>(p, tz, x, y, lanes);
+            return;
+        }
+    }
+    step_pair_body<SID, ST, COLL, PAT, false>(p, tz, x, y, lanes);
 }
 
 template <int SID, int ST, int COLL, int PAT>
