@@ -15,8 +15,11 @@ them.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference|lettuce]
 
-``--impl reference`` times the CPU oracle (a C restatement of lettuce's torch
-step) on this host's cores instead; ``--impl lettuce`` times lettuce itself
+``cpu_baseline`` is the CPU oracle (a C restatement of lettuce's torch step)
+on this host's cores; ``lettuce_cpu`` is lettuce's own torch CPU path on
+the same cores in the same run (lettuce installed in baseline/_ref).
+
+``--impl reference`` times the CPU oracle on this host's cores instead; ``--impl lettuce`` times lettuce itself
 (installed in baseline/_ref): its generated cuda_native kernel and its torch
 path on the GPU, and its torch path on the host cores.
 """
@@ -353,7 +356,8 @@ def run_lettuce(args, world, rank):
         torch.cuda.empty_cache()
         return out
 
-    if torch.cuda.is_available():
+    cpu_only = os.environ.get("LGB_LETTUCE_CPU_ONLY") == "1"
+    if torch.cuda.is_available() and not cpu_only:
         peak, _ = peaks()
         line["cuda_native"] = gpu_leg(True)
         line["cuda_native"].update(how)
@@ -394,6 +398,25 @@ def run_lettuce(args, world, rank):
                                    f"{nthreads} intra-op threads"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def lettuce_cpu_sample():
+    """lettuce's own torch CPU path (``Context(device='cpu', use_native=False)``)
+    on the headline workload, 256^3 float32, timed on this host's cores in a
+    child process (``--impl lettuce`` with its GPU legs off): 2 steps after
+    one warm-up step. None where lettuce is not installed in baseline/_ref."""
+    if not os.path.isfile(os.path.join(ROOT, "baseline", "_ref", "lettuce", "__init__.py")):
+        return None
+    env = dict(os.environ, LGB_LETTUCE_CPU_ONLY="1")
+    try:
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "lettuce",
+                            "--steps", "2", "--warmup", "1"], env=env, capture_output=True,
+                           text=True, timeout=600)
+        leg = json.loads(r.stdout.strip().splitlines()[-1])["torch_cpu"]
+    except (subprocess.SubprocessError, ValueError, KeyError, IndexError) as e:
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    return {"value": leg["mlups"], "unit": UNIT, "cores": leg["cores"],
+            "kind": "lettuce torch CPU path", "sample": leg["sample"]}
 
 
 def time_variant(lt, torch, storage, pattern, steps, warmup, device):
@@ -1000,12 +1023,14 @@ def run_ours(args, world, rank, local):
         configs = measure_configs(lt, torch, device, peak)
 
     cpu = None
+    lettuce_cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         mlups_cpu, s, n, dt = oracle_mlups([256, 256, 64], args.cpu_seconds, nthreads)
         cpu = {"value": round(mlups_cpu, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"{s} steps of the oracle (C restatement of lettuce's torch step, "
                          f"float32) on a 256x256x64 periodic TGV crop, {dt:.1f} s"}
+        lettuce_cpu = lettuce_cpu_sample()
 
     if rank != 0:
         return 0
@@ -1034,6 +1059,7 @@ def run_ours(args, world, rank, local):
                         "flow.download(pinned host field)",
                 "phases": phases},
         "cpu_baseline": cpu,
+        "lettuce_cpu": lettuce_cpu,
         "configs": configs,
         "clocks": clocks,
         "gpu_launches": args.steps,
