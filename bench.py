@@ -356,6 +356,23 @@ def run_lettuce(args, world, rank):
         torch.cuda.empty_cache()
         return out
 
+    # lettuce's torch path on the host cores, bounded sample (first: in a
+    # process that has initialised CUDA it measured half this rate)
+    nthreads = os.cpu_count() or 1
+    torch.set_num_threads(nthreads)
+    cpu_res = [int(x) for x in os.environ.get("LGB_LETTUCE_CPU_GRID", "256,256,256").split(",")]
+    flow, sim, _ = build("cpu", False, cpu_res)
+    sim(1)
+    t0 = time.perf_counter()
+    ret = sim(3)
+    dt = time.perf_counter() - t0
+    line["torch_cpu"] = {"mlups": round(3 * int(np.prod(cpu_res)) / dt / 1e6, 3),
+                         "lettuce_return_mlups": round(float(ret), 3), "cores": nthreads,
+                         "sample": f"3 steps on {cpu_res[0]}x{cpu_res[1]}x{cpu_res[2]} after one "
+                                   f"warm-up step, torch {torch.__version__}, "
+                                   f"{nthreads} intra-op threads"}
+    del flow, sim
+
     cpu_only = os.environ.get("LGB_LETTUCE_CPU_ONLY") == "1"
     if torch.cuda.is_available() and not cpu_only:
         peak, _ = peaks()
@@ -382,20 +399,6 @@ def run_lettuce(args, world, rank):
             mine = ours_flow.f.detach().cpu().double()
             line["cuda_native"]["max_rel_diff_vs_lettuce_gb300_32cube_10_steps"] = float(
                 ((got - mine).abs().max() / mine.abs().max()).item())
-    # lettuce's torch path on the host cores, bounded sample
-    nthreads = os.cpu_count() or 1
-    torch.set_num_threads(nthreads)
-    cpu_res = [int(x) for x in os.environ.get("LGB_LETTUCE_CPU_GRID", "256,256,256").split(",")]
-    flow, sim, _ = build("cpu", False, cpu_res)
-    sim(1)
-    t0 = time.perf_counter()
-    ret = sim(2)
-    dt = time.perf_counter() - t0
-    line["torch_cpu"] = {"mlups": round(2 * int(np.prod(cpu_res)) / dt / 1e6, 3),
-                         "lettuce_return_mlups": round(float(ret), 3), "cores": nthreads,
-                         "sample": f"2 steps on {cpu_res[0]}x{cpu_res[1]}x{cpu_res[2]} after one "
-                                   f"warm-up step, torch {torch.__version__}, "
-                                   f"{nthreads} intra-op threads"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -403,14 +406,14 @@ def run_lettuce(args, world, rank):
 def lettuce_cpu_sample():
     """lettuce's own torch CPU path (``Context(device='cpu', use_native=False)``)
     on the headline workload, 256^3 float32, timed on this host's cores in a
-    child process (``--impl lettuce`` with its GPU legs off): 2 steps after
+    child process (``--impl lettuce`` with its GPU legs off): 3 steps after
     one warm-up step. None where lettuce is not installed in baseline/_ref."""
     if not os.path.isfile(os.path.join(ROOT, "baseline", "_ref", "lettuce", "__init__.py")):
         return None
     env = dict(os.environ, LGB_LETTUCE_CPU_ONLY="1")
     try:
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "lettuce",
-                            "--steps", "2", "--warmup", "1"], env=env, capture_output=True,
+                            "--steps", "3", "--warmup", "1"], env=env, capture_output=True,
                            text=True, timeout=600)
         leg = json.loads(r.stdout.strip().splitlines()[-1])["torch_cpu"]
     except (subprocess.SubprocessError, ValueError, KeyError, IndexError) as e:
