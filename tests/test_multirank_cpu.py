@@ -57,3 +57,31 @@ def test_reference_arm_under_torchrun_prints_once(lgb, oracle):
     assert rec["impl"] == "reference" and rec["unit"] == "MLUPS" and rec["value"] > 0
     assert rec["cpu_baseline"]["kind"] == "port"
     assert rec["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_lettuce_arm_cpu_leg():
+    """``bench.py --impl lettuce`` with its GPU legs off: lettuce's own torch
+    CPU path on a small grid, one JSON line with the sample stated; and the
+    main line's ``lettuce_cpu`` entry built from it. Skipped when lettuce
+    is not installed in baseline/_ref."""
+    if not os.path.isfile(os.path.join(ROOT, "baseline", "_ref", "lettuce", "__init__.py")):
+        pytest.skip("lettuce is not installed in baseline/_ref")
+    env = dict(os.environ, LGB_LETTUCE_CPU_ONLY="1", LGB_LETTUCE_CPU_GRID="12,10,8")
+    cmd = [sys.executable, "bench.py", "--impl", "lettuce", "--steps", "3", "--warmup", "1"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    rec = json.loads(lines[0])
+    assert rec["impl"] == "lettuce" and rec["lettuce"]["version"]
+    leg = rec["torch_cpu"]
+    assert leg["mlups"] > 0 and leg["cores"] >= 1 and "12x10x8" in leg["sample"]
+    assert "cuda_native" not in rec
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ["LGB_LETTUCE_CPU_GRID"] = "12,10,8"
+    try:
+        got = bench.lettuce_cpu_sample()
+    finally:
+        del os.environ["LGB_LETTUCE_CPU_GRID"]
+    assert got["kind"] == "lettuce torch CPU path" and got["value"] > 0
