@@ -372,7 +372,9 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
 // memory 126.1k (50), capped at 48 140.0k (no spills), at 44 136.6k (20
 // bytes of spills), at 40 134.8k (48 bytes); with the next pair's words
 // copied asynchronously (cp.async, 4 bytes each) into a two-stage
-// shared-memory buffer while the current pair collides, 110.8k.
+// shared-memory buffer while the current pair collides, 110.8k. Float32:
+// 76.2k uncapped (64 registers), 84.4k at 40, 82.8k at 32 (20 bytes of
+// spills).
 #ifndef LGB_BATCH_16BIT_2D_MAXREG
 #define LGB_BATCH_16BIT_2D_MAXREG 48
 #endif
