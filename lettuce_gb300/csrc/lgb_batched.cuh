@@ -94,13 +94,28 @@ struct BatchParams {
 #define LGB_BATCH_LEAN 1
 #endif
 
-// a tile of a 16-bit domain as its pair loop reads it
-struct TilePairs {
-    uint64_t word_offset;  // the domain's first 32-bit word in the pool
+// a tile of a 16-bit domain as its pair loop reads it: three 16-byte
+// groups, each read with one shared-memory load where it is used
+struct alignas(16) TilePairs {
     uint32_t X, Y, Zh, Nh; // grid, words per row, words per population plane
-    uint32_t end;          // one past the tile's last pair (row Zh + word)
     float f_omega, f_one_minus_omega, f_inv_2tp, f_inv_2tm;
+    uint32_t word_lo, word_hi; // the domain's first 32-bit word in the pool
+    uint32_t end;              // one past the tile's last pair (row Zh + word)
+    uint32_t step_rows;        // blockDim / Zh: whole rows a thread advances
 };
+
+// The pair loop reads the tile's values as 16-byte shared-memory loads (1)
+// or field by field through a volatile reference (0).
+#ifndef LGB_BATCH_VEC_TILE
+#define LGB_BATCH_VEC_TILE 1
+#endif
+__device__ __forceinline__ uint4 lds_u4(const void *ptr) {
+    uint4 v;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(ptr);
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+    return v;
+}
 
 // the pull step of the pairs t2, t2 + blockDim, ... below ts.end of a tile
 // (pair index = row Zh + word), the tile's values read from shared memory
@@ -123,8 +138,8 @@ __device__ __forceinline__ void tile_pairs_pull(const BatchParams &p, const vola
         float2 h[S::Q];
         {
             const uint32_t X = ts.X, Y = ts.Y, Zh = ts.Zh, Nh = ts.Nh;
-            const uint32_t *__restrict__ fin =
-                static_cast<const uint32_t *>(p.f_in) + ts.word_offset;
+            const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in) +
+                                               (((uint64_t)ts.word_hi << 32) | ts.word_lo);
             const uint32_t xm = x == 0 ? X - 1 : x - 1, xp = x + 1 == X ? 0 : x + 1;
             const uint32_t ym = y == 0 ? Y - 1 : y - 1, yp = y + 1 == Y ? 0 : y + 1;
             const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
@@ -157,7 +172,8 @@ __device__ __forceinline__ void tile_pairs_pull(const BatchParams &p, const vola
         }
         {
             const uint32_t Nh = ts.Nh;
-            uint32_t *fout = static_cast<uint32_t *>(p.f_out) + ts.word_offset +
+            uint32_t *fout = static_cast<uint32_t *>(p.f_out) +
+                             (((uint64_t)ts.word_hi << 32) | ts.word_lo) +
                              (x * ts.Y + y) * ts.Zh + tz;
 #pragma unroll
             for (int q = 0; q < S::Q; ++q) fout[(size_t)q * Nh] = P::encode(h[q]);
@@ -170,6 +186,77 @@ __device__ __forceinline__ void tile_pairs_pull(const BatchParams &p, const vola
             tz -= Zh;
             if (++y == ts.Y) { y = 0; ++x; }
         }
+    }
+}
+
+// tile_pairs_pull reading the tile's values in 16-byte groups; the next
+// pair lies blockDim pairs on: ts.step_rows whole rows plus blockDim mod Zh
+// words (no division, no per-row loop)
+template <int SID, int ST, int COLL, bool PADDED>
+__device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const TilePairs &ts,
+                                                    uint32_t t2) {
+    using S = Stencil<SID>;
+    using P = Pack16<ST>;
+    const void *g_grid = &ts.X, *g_rates = &ts.f_omega, *g_tile = &ts.word_lo;
+    uint32_t tz, x, y;
+    {
+        const uint4 gr = lds_u4(g_grid);
+        const uint32_t row = t2 / gr.z;
+        tz = t2 - row * gr.z;
+        x = row / gr.y;
+        y = row - x * gr.y;
+    }
+    while (true) {
+        float2 h[S::Q];
+        {
+            const uint4 gr = lds_u4(g_grid), tl = lds_u4(g_tile);
+            const uint32_t X = gr.x, Y = gr.y, Zh = gr.z, Nh = gr.w;
+            const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in) +
+                                               (((uint64_t)tl.y << 32) | tl.x);
+            const uint32_t xm = x == 0 ? X - 1 : x - 1, xp = x + 1 == X ? 0 : x + 1;
+            const uint32_t ym = y == 0 ? Y - 1 : y - 1, yp = y + 1 == Y ? 0 : y + 1;
+            const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) {
+                const int dx = -ix<S>(q), dy = -iy<S>(q);
+                const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
+                const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
+                const uint32_t *r = fin + (size_t)q * Nh + (a * Y + b) * Zh;
+                uint32_t w;
+                if constexpr (PADDED) w = load_pair_padded(r, tz, Zh, -iz<S>(q));
+                else w = load_pair(r, tz, tzm, tzp, -iz<S>(q));
+                h[q] = P::decode(w);
+            }
+        }
+        {
+            const uint4 rt = lds_u4(g_rates);
+            CollideParams cp;
+            cp.f_omega = __uint_as_float(rt.x);
+            cp.f_one_minus_omega = __uint_as_float(rt.y);
+            cp.f_inv_2tp = __uint_as_float(rt.z);
+            cp.f_inv_2tm = __uint_as_float(rt.w);
+            collide_shifted<S, Lane2, COLL>(h, cp);
+        }
+        const uint4 gr = lds_u4(g_grid), tl = lds_u4(g_tile);
+        if (p.status) {
+            float2 r = h[0];
+#pragma unroll
+            for (int q = 1; q < S::Q; ++q) r = Lane2::add(r, h[q]);
+            if (!isfinite(r.x) || ((!PADDED || tz + 1 < gr.z) && !isfinite(r.y)))
+                atomicOr(p.status, 1u);
+        }
+        {
+            uint32_t *fout = static_cast<uint32_t *>(p.f_out) + (((uint64_t)tl.y << 32) | tl.x) +
+                             (x * gr.y + y) * gr.z + tz;
+#pragma unroll
+            for (int q = 0; q < S::Q; ++q) fout[(size_t)q * gr.w] = P::encode(h[q]);
+        }
+        t2 += blockDim.x;
+        if (t2 >= tl.z) break;
+        tz += blockDim.x - tl.w * gr.z;
+        y += tl.w;
+        if (tz >= gr.z) { tz -= gr.z; ++y; }
+        while (y >= gr.y) { y -= gr.y; ++x; }
     }
 }
 
@@ -240,12 +327,15 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
                 s_pairs.f_one_minus_omega = c.f_one_minus_omega;
                 s_pairs.f_inv_2tp = c.f_inv_2tp;
                 s_pairs.f_inv_2tm = c.f_inv_2tm;
-                s_pairs.word_offset = (uint64_t)dom.offset >> 1;
+                const uint64_t word_offset = (uint64_t)dom.offset >> 1;
+                s_pairs.word_lo = (uint32_t)word_offset;
+                s_pairs.word_hi = (uint32_t)(word_offset >> 32);
                 s_pairs.X = r[0];
                 s_pairs.Y = r[1];
                 s_pairs.Zh = pitch >> 1;
                 s_pairs.Nh = (uint32_t)(n_alloc >> 1);
                 s_pairs.end = (uint32_t)tile.row_end * (pitch >> 1);
+                s_pairs.step_rows = blockDim.x / (pitch >> 1);
             }
         }
         __syncthreads();
@@ -255,8 +345,13 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
             if (padded || ((r[2] & 1u) == 0 && (dom.offset & 1) == 0)) {
                 const uint32_t t2 = (uint32_t)tile.row_begin * (pitch >> 1) + threadIdx.x;
                 if (t2 < (uint32_t)tile.row_end * (pitch >> 1)) {
-                    if (padded) tile_pairs_pull<SID, ST, COLL, true>(p, s_pairs, t2);
-                    else tile_pairs_pull<SID, ST, COLL, false>(p, s_pairs, t2);
+                    if constexpr (LGB_BATCH_VEC_TILE) {
+                        if (padded) tile_pairs_pull_vec<SID, ST, COLL, true>(p, s_pairs, t2);
+                        else tile_pairs_pull_vec<SID, ST, COLL, false>(p, s_pairs, t2);
+                    } else {
+                        if (padded) tile_pairs_pull<SID, ST, COLL, true>(p, s_pairs, t2);
+                        else tile_pairs_pull<SID, ST, COLL, false>(p, s_pairs, t2);
+                    }
                 }
                 continue;
             }
