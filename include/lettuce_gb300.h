@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LGB_ABI_VERSION 4
+#define LGB_ABI_VERSION 5
 #define LGB_MAX_SUBSTEPS 8
 
 /* stencils (lettuce/ext/_stencil/d1q3.py, d2q9.py, d3q15.py, d3q19.py, d3q27.py) */
@@ -345,6 +345,13 @@ typedef struct {
     uint32_t *status;    /* optional; bit 0 non-finite density, bit 1 a tile
                             outside its domain or the pool, or a pitch the
                             domain's format does not accept (skipped) */
+    const float *rates;  /* optional device table, 16-byte aligned, four floats
+                            per domain: (float) (1 / tau), (float) (1 - 1 / tau),
+                            (float) (1 / (2 tau)), (float) (1 / (2 tau_minus)),
+                            each rounded once from the float64 value. With it the
+                            float32 and 16-bit batches form no float64 quotient in
+                            the kernel; NULL: formed per tile from tau (float64
+                            batches always do). */
 } lgb_batch_desc;
 
 /* Host-only: cut every domain into tiles of whole rows holding about

@@ -41,7 +41,8 @@ class BatchDesc(ctypes.Structure):
                 ("threads", ctypes.c_int32), ("blocks", ctypes.c_int32),
                 ("domains", ctypes.c_void_p), ("tiles", ctypes.c_void_p),
                 ("f_in", ctypes.c_void_p), ("f_out", ctypes.c_void_p),
-                ("pool_elements", ctypes.c_int64), ("status", ctypes.c_void_p)]
+                ("pool_elements", ctypes.c_int64), ("status", ctypes.c_void_p),
+                ("rates", ctypes.c_void_p)]
 
 
 def _bind(L):
@@ -138,6 +139,12 @@ class BatchedSimulation:
             self._domain_view(self._pools[0], b).copy_(fl.f_raw)
         self._cur = 0
         self._domains_dev = torch.from_numpy(dom.view(np.uint8).copy()).to(dev)
+        # the float32 rates of every domain, rounded once from the float64
+        # quotients (the kernel's float32 and 16-bit collisions use these)
+        omega = 1.0 / dom["tau"]
+        rates = np.stack([omega, 1.0 - omega, 1.0 / (2.0 * dom["tau"]),
+                          1.0 / (2.0 * dom["tau_minus"])], axis=1).astype(np.float32)
+        self._rates_dev = torch.from_numpy(np.ascontiguousarray(rates)).to(dev)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._graph = None
         self._graph_key = None
@@ -190,6 +197,7 @@ class BatchedSimulation:
         d.f_out = dst.data_ptr()
         d.pool_elements = self.pool_elements
         d.status = self._status.data_ptr()
+        d.rates = self._rates_dev.data_ptr() if self._rates_dev is not None else None
         return d
 
     def _launch(self, src, dst, stream):

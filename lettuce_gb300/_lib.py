@@ -12,7 +12,7 @@ import threading
 
 from . import build as _build
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 LINK_FORCE_BLOCK = 256  # LGB_LINK_FORCE_BLOCK
 MAX_SUBSTEPS = 8
 REDUCE_FIELDS = 5

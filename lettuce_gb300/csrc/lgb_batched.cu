@@ -103,6 +103,9 @@ int lgb_batched_step(const lgb_batch_desc *d, void *stream) {
     p.n_tiles = d->n_tiles;
     p.pool_elements = d->pool_elements;
     p.status = d->status;
+    if (d->rates && (reinterpret_cast<uintptr_t>(d->rates) & 15u))
+        return bfail("lgb_batched_step: rates must be 16-byte aligned");
+    p.rates = d->storage == LGB_F64 ? nullptr : reinterpret_cast<const float4 *>(d->rates);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaErrorInvalidValue;
     switch (d->stencil) {

@@ -82,6 +82,7 @@ struct BatchParams {
     int32_t n_tiles;
     int64_t pool_elements;
     uint32_t *status;
+    const float4 *rates;  // per domain, formed on the host (or null)
 };
 
 // The 16-bit pair loop keeps its tile's domain in shared memory and reads
@@ -271,6 +272,7 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
     const T *__restrict__ pool_in = static_cast<const T *>(p.f_in);
     T *pool_out = static_cast<T *>(p.f_out);
     __shared__ double s_rates[3];
+    __shared__ float s_frates[4];
     __shared__ TilePairs s_pairs;
     for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
         const lgb_batch_tile tile = p.tiles[t];
@@ -314,15 +316,34 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
         // branches above are uniform and every thread reaches both barriers.
         __syncthreads();  // the previous tile's rates have been read
         if (threadIdx.x == 0) {
-            s_rates[0] = 1.0 / dom.tau;
-            s_rates[1] = 1.0 / (2.0 * dom.tau);
-            s_rates[2] = 1.0 / (2.0 * dom.tau_minus);
-            if constexpr (HSPACE && LGB_BATCH_LEAN) {
-                CollideParams c;
+            // the float32 rates the collisions of the float32 and 16-bit
+            // formats use: from the host's table, or rounded here from the
+            // float64 quotients (the same values); the float32 collision
+            // takes its rates back from the doubles exactly
+            CollideParams c;
+            if (p.rates) {
+                const float4 fr = p.rates[tile.domain];
+                c.f_omega = fr.x;
+                c.f_one_minus_omega = fr.y;
+                c.f_inv_2tp = fr.z;
+                c.f_inv_2tm = fr.w;
+                s_rates[0] = (double)fr.x;
+                s_rates[1] = (double)fr.z;
+                s_rates[2] = (double)fr.w;
+            } else {
+                s_rates[0] = 1.0 / dom.tau;
+                s_rates[1] = 1.0 / (2.0 * dom.tau);
+                s_rates[2] = 1.0 / (2.0 * dom.tau_minus);
                 c.omega = s_rates[0];
                 c.inv_2tp = s_rates[1];
                 c.inv_2tm = s_rates[2];
                 set_float_rates(c);
+            }
+            s_frates[0] = c.f_omega;
+            s_frates[1] = c.f_one_minus_omega;
+            s_frates[2] = c.f_inv_2tp;
+            s_frates[3] = c.f_inv_2tm;
+            if constexpr (HSPACE && LGB_BATCH_LEAN) {
                 s_pairs.f_omega = c.f_omega;
                 s_pairs.f_one_minus_omega = c.f_one_minus_omega;
                 s_pairs.f_inv_2tp = c.f_inv_2tp;
@@ -361,7 +382,10 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
         cp.inv_2tp = s_rates[1];
         cp.inv_2tm = s_rates[2];
         cp.beta = s_rates[1];
-        set_float_rates(cp);
+        cp.f_omega = s_frates[0];
+        cp.f_one_minus_omega = s_frates[1];
+        cp.f_inv_2tp = s_frates[2];
+        cp.f_inv_2tm = s_frates[3];
         const T *__restrict__ fin = pool_in + dom.offset;
         T *fout = pool_out + dom.offset;
         // a thread's cells advance by blockDim along the tile's rows: the
@@ -467,11 +491,13 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
 // memory 126.1k (50), capped at 48 140.0k (no spills), at 44 136.6k (20
 // bytes of spills), at 40 134.8k (48 bytes); reading the tile's values as
 // 16-byte loads with a division-free advance, capped at 48, 143.0k against
-// 140.3k (at 44: 20 bytes of spills); with the next pair's words
+// 140.3k (at 44: 20 bytes of spills); with the domains' float32 rates
+// formed on the host (no float64 quotient per tile) 145.4k; with the next
+// pair's words
 // copied asynchronously (cp.async, 4 bytes each) into a two-stage
 // shared-memory buffer while the current pair collides, 110.8k. Float32:
 // 76.2k uncapped (64 registers), 84.4k at 40, 82.8k at 32 (20 bytes of
-// spills).
+// spills); 85.0k with the host's rates.
 #ifndef LGB_BATCH_16BIT_2D_MAXREG
 #define LGB_BATCH_16BIT_2D_MAXREG 48
 #endif

@@ -168,11 +168,12 @@ def test_batch_struct_layouts_match_header(tmp_path, lgb):
     src = tmp_path / "probe_batch.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "lettuce_gb300.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu\\n\","
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\","
         " sizeof(lgb_batch_domain), offsetof(lgb_batch_domain, tau),"
         " sizeof(lgb_batch_tile), sizeof(lgb_batch_desc),"
         " offsetof(lgb_batch_desc, domains), offsetof(lgb_batch_desc, f_out),"
-        " offsetof(lgb_batch_desc, pool_elements), offsetof(lgb_batch_desc, status));"
+        " offsetof(lgb_batch_desc, pool_elements), offsetof(lgb_batch_desc, status),"
+        " offsetof(lgb_batch_desc, rates));"
         "return 0;}\n")
     exe = tmp_path / "probe_batch"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)],
@@ -181,7 +182,8 @@ def test_batch_struct_layouts_match_header(tmp_path, lgb):
                                           check=True).stdout.split()]
     assert got == [DOMAIN_DTYPE.itemsize, DOMAIN_DTYPE.fields["tau"][1], TILE_DTYPE.itemsize,
                    ctypes.sizeof(BatchDesc), BatchDesc.domains.offset, BatchDesc.f_out.offset,
-                   BatchDesc.pool_elements.offset, BatchDesc.status.offset]
+                   BatchDesc.pool_elements.offset, BatchDesc.status.offset,
+                   BatchDesc.rates.offset]
 
 
 def test_init_and_enstrophy_validation(lgb):

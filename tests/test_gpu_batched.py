@@ -32,6 +32,23 @@ def test_batch_equals_single_domain_runs(lgb, dtype, storage, persistent):
         assert fl.i == 13
 
 
+@pytest.mark.parametrize("storage", [None, "fp16_shifted"])
+def test_host_rates_equal_kernel_rates(lgb, storage):
+    """the per-domain float32 rates formed on the host (lgb_batch_desc.rates)
+    and those the kernel forms from tau without the table give the same
+    fields bit for bit"""
+    a, ca = _batch(storage)
+    b, cb = _batch(storage)
+    sa = lt.BatchedSimulation(a, ca, tile_cells=500, threads=128)
+    sb = lt.BatchedSimulation(b, cb, tile_cells=500, threads=128)
+    assert sa._rates_dev is not None
+    sb._rates_dev = None
+    sa(9, use_graph=False)
+    sb(9, use_graph=False)
+    for x, y in zip(a, b):
+        assert torch.equal(x.f_raw, y.f_raw)
+
+
 def test_batch_against_oracle(lgb, oracle):
     flows, colls = _batch(None, torch.float64, n=5)
     f0 = [to_np(fl.f) for fl in flows]
