@@ -103,6 +103,9 @@ struct alignas(16) TilePairs {
     uint32_t word_lo, word_hi; // the domain's first 32-bit word in the pool
     uint32_t end;              // one past the tile's last pair (row Zh + word)
     uint32_t step_rows;        // blockDim / Zh: whole rows a thread advances
+    uint32_t begin;            // the tile's first pair
+    uint32_t kind;             // 0: skip the tile, 1: even rows, 2: padded odd rows
+    uint32_t unused[2];
 };
 
 // The pair loop reads the tile's values as 16-byte shared-memory loads (1)
@@ -261,6 +264,72 @@ __device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const 
     }
 }
 
+// One thread reads tile t and its domain, checks them as the per-thread
+// path below does, and fills the block's TilePairs (kind 0 and status bit 1
+// for a tile it refuses). The 16-bit pair loop needs nothing else of them.
+template <int SID>
+__device__ __forceinline__ void setup_tile_pairs(const BatchParams &p, const int t, TilePairs &ts) {
+    using S = Stencil<SID>;
+    ts.kind = 0;
+    const lgb_batch_tile tile = p.tiles[t];
+    if (tile.domain < 0 || tile.domain >= p.n_domains) {
+        if (p.status) atomicOr(p.status, 2u);
+        return;
+    }
+    const lgb_batch_domain dom = p.domains[tile.domain];
+    const int d = S::D;
+    uint32_t r[3] = {1, 1, 1};
+    bool ok = true;
+    for (int i = 0; i < d; ++i) {
+        ok = ok && dom.res[i] > 0;
+        r[3 - d + i] = (uint32_t)dom.res[i];
+    }
+    const uint32_t pitch = dom.pitch == 0 ? r[2] : (uint32_t)dom.pitch;
+    const bool padded = pitch != r[2];
+    ok = ok && dom.pitch >= 0 &&
+         (!padded || ((r[2] & 1u) && pitch == r[2] + 1 && (dom.offset & 1) == 0));
+    const uint64_t n_alloc = (uint64_t)r[0] * r[1] * pitch;
+    ok = ok && n_alloc < (1ull << 32) && dom.offset >= 0 &&
+         (uint64_t)dom.offset + (uint64_t)S::Q * n_alloc <= (uint64_t)p.pool_elements &&
+         tile.row_begin >= 0 && tile.row_begin <= tile.row_end &&
+         (uint64_t)tile.row_end <= (uint64_t)r[0] * r[1] && dom.tau > 0.0;
+    // rows of whole 32-bit words: padded odd rows, or even rows at an even offset
+    ok = ok && (padded || ((r[2] & 1u) == 0 && (dom.offset & 1) == 0));
+    if (!ok) {
+        if (p.status) atomicOr(p.status, 2u);
+        return;
+    }
+    CollideParams c;
+    if (p.rates) {
+        const float4 fr = p.rates[tile.domain];
+        c.f_omega = fr.x;
+        c.f_one_minus_omega = fr.y;
+        c.f_inv_2tp = fr.z;
+        c.f_inv_2tm = fr.w;
+    } else {
+        c.omega = 1.0 / dom.tau;
+        c.inv_2tp = 1.0 / (2.0 * dom.tau);
+        c.inv_2tm = 1.0 / (2.0 * dom.tau_minus);
+        set_float_rates(c);
+    }
+    ts.f_omega = c.f_omega;
+    ts.f_one_minus_omega = c.f_one_minus_omega;
+    ts.f_inv_2tp = c.f_inv_2tp;
+    ts.f_inv_2tm = c.f_inv_2tm;
+    const uint64_t word_offset = (uint64_t)dom.offset >> 1;
+    const uint32_t Zh = pitch >> 1;
+    ts.word_lo = (uint32_t)word_offset;
+    ts.word_hi = (uint32_t)(word_offset >> 32);
+    ts.X = r[0];
+    ts.Y = r[1];
+    ts.Zh = Zh;
+    ts.Nh = (uint32_t)(n_alloc >> 1);
+    ts.end = (uint32_t)tile.row_end * Zh;
+    ts.step_rows = blockDim.x / Zh;
+    ts.begin = (uint32_t)tile.row_begin * Zh;
+    ts.kind = padded ? 2u : 1u;
+}
+
 // the batched step (one launch over every tile of the batch)
 template <int SID, int ST, int COLL>
 __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
@@ -275,6 +344,22 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
     __shared__ float s_frates[4];
     __shared__ TilePairs s_pairs;
     for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
+        if constexpr (HSPACE && LGB_BATCH_LEAN && LGB_BATCH_VEC_TILE) {
+            // the 16-bit pair loop: one thread sets the tile up (the loop
+            // bounds are uniform, so every thread reaches both barriers)
+            if (t != (int)blockIdx.x) __syncthreads();  // the previous tile is read
+            if (threadIdx.x == 0) setup_tile_pairs<SID>(p, t, s_pairs);
+            __syncthreads();
+            const uint4 bk = lds_u4(&s_pairs.begin);
+            if (bk.y != 0) {
+                const uint32_t t2 = bk.x + threadIdx.x;
+                if (t2 < lds_u4(&s_pairs.word_lo).z) {
+                    if (bk.y == 2u) tile_pairs_pull_vec<SID, ST, COLL, true>(p, s_pairs, t2);
+                    else tile_pairs_pull_vec<SID, ST, COLL, false>(p, s_pairs, t2);
+                }
+            }
+            continue;
+        }
         const lgb_batch_tile tile = p.tiles[t];
         if (tile.domain < 0 || tile.domain >= p.n_domains) {
             if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
@@ -492,7 +577,8 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
 // bytes of spills), at 40 134.8k (48 bytes); reading the tile's values as
 // 16-byte loads with a division-free advance, capped at 48, 143.0k against
 // 140.3k (at 44: 20 bytes of spills); with the domains' float32 rates
-// formed on the host (no float64 quotient per tile) 145.4k; with the next
+// formed on the host (no float64 quotient per tile) 145.4k, and with one
+// thread setting each tile up for the block 146.7k; with the next
 // pair's words
 // copied asynchronously (cp.async, 4 bytes each) into a two-stage
 // shared-memory buffer while the current pair collides, 110.8k. Float32:
