@@ -202,13 +202,20 @@ __device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const 
     using S = Stencil<SID>;
     using P = Pack16<ST>;
     const void *g_grid = &ts.X, *g_rates = &ts.f_omega, *g_tile = &ts.word_lo;
-    uint32_t tz, x, y;
+    // FLAT: a one- or two-dimensional grid (X = 1): the row is y, and no
+    // pair of the tile lies past the last row
+    constexpr bool FLAT = S::D < 3;
+    uint32_t tz, x = 0, y;
     {
         const uint4 gr = lds_u4(g_grid);
         const uint32_t row = t2 / gr.z;
         tz = t2 - row * gr.z;
-        x = row / gr.y;
-        y = row - x * gr.y;
+        if constexpr (FLAT) {
+            y = row;
+        } else {
+            x = row / gr.y;
+            y = row - x * gr.y;
+        }
     }
     while (true) {
         float2 h[S::Q];
@@ -225,7 +232,7 @@ __device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const 
                 const int dx = -ix<S>(q), dy = -iy<S>(q);
                 const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
                 const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
-                const uint32_t *r = fin + (size_t)q * Nh + (a * Y + b) * Zh;
+                const uint32_t *r = fin + (size_t)q * Nh + ((FLAT ? 0u : a * Y) + b) * Zh;
                 uint32_t w;
                 if constexpr (PADDED) w = load_pair_padded(r, tz, Zh, -iz<S>(q));
                 else w = load_pair(r, tz, tzm, tzp, -iz<S>(q));
@@ -251,7 +258,7 @@ __device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const 
         }
         {
             uint32_t *fout = static_cast<uint32_t *>(p.f_out) + (((uint64_t)tl.y << 32) | tl.x) +
-                             (x * gr.y + y) * gr.z + tz;
+                             ((FLAT ? 0u : x * gr.y) + y) * gr.z + tz;
 #pragma unroll
             for (int q = 0; q < S::Q; ++q) fout[(size_t)q * gr.w] = P::encode(h[q]);
         }
@@ -260,7 +267,9 @@ __device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const 
         tz += blockDim.x - tl.w * gr.z;
         y += tl.w;
         if (tz >= gr.z) { tz -= gr.z; ++y; }
-        while (y >= gr.y) { y -= gr.y; ++x; }
+        if constexpr (!FLAT) {
+            while (y >= gr.y) { y -= gr.y; ++x; }
+        }
     }
 }
 
@@ -578,7 +587,8 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
 // 16-byte loads with a division-free advance, capped at 48, 143.0k against
 // 140.3k (at 44: 20 bytes of spills); with the domains' float32 rates
 // formed on the host (no float64 quotient per tile) 145.4k, and with one
-// thread setting each tile up for the block 146.7k; with the next
+// thread setting each tile up for the block 146.7k, and with the
+// two-dimensional grids' x dropped from the pair loop 148.1k; with the next
 // pair's words
 // copied asynchronously (cp.async, 4 bytes each) into a two-stage
 // shared-memory buffer while the current pair collides, 110.8k. Float32:
