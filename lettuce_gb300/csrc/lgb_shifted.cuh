@@ -9,7 +9,9 @@
 // The arithmetic is written once over a lane type L: L = Lane1 (one cell per
 // thread, float) or Lane2 (two cells per thread, float2 with the packed
 // f32x2 instructions of sm_100+). Both give bit-identical per-cell results
-// because every operation is an explicit round-to-nearest intrinsic AND no
+// because every operation is an explicit round-to-nearest intrinsic (the
+// reciprocal of the density: one approximate instruction, the same in both)
+// AND no
 // product is ever an operand of an add or subtract: the compiler fuses a
 // packed multiply into a following packed add (the scalar __fmul_rn is never
 // fused), so every multiply-add here is written as an explicit FMA, and the
@@ -23,6 +25,21 @@
 
 namespace lgb {
 
+// 1 / rho on one- and two-dimensional stencils: the hardware's approximate
+// reciprocal (__fdividef, within 2 ulp; the same instruction in both lane
+// types, so they stay bit-identical) (1), or the correctly rounded
+// __frcp_rn (0); three-dimensional stencils always take __frcp_rn. Far
+// below the 16-bit storage's rounding either way. Measured: the batched
+// D2Q9 fp16 TRT step 147.1k -> 150.9k MLUPS; the D3Q19 two-cell kernels
+// lost with it (pull 82.6k -> 81.1k, AA pair 76.6k -> 71.8k: the AA odd
+// step spilled 208 bytes instead of 40).
+#ifndef LGB_SHIFTED_FAST_RCP_2D
+#define LGB_SHIFTED_FAST_RCP_2D 1
+#endif
+__device__ __forceinline__ float shifted_rcp(float a, bool fast) {
+    return fast ? __fdividef(1.0f, a) : __frcp_rn(a);
+}
+
 struct Lane1 {
     using V = float;
     static __device__ __forceinline__ V set(float a) { return a; }
@@ -30,7 +47,7 @@ struct Lane1 {
     static __device__ __forceinline__ V sub(V a, V b) { return __fsub_rn(a, b); }
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ V fma(V a, V b, V c) { return __fmaf_rn(a, b, c); }
-    static __device__ __forceinline__ V rcp(V a) { return __frcp_rn(a); }
+    static __device__ __forceinline__ V rcp(V a, bool fast) { return shifted_rcp(a, fast); }
 };
 
 struct Lane2 {
@@ -42,7 +59,9 @@ struct Lane2 {
     }
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
     static __device__ __forceinline__ V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
-    static __device__ __forceinline__ V rcp(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+    static __device__ __forceinline__ V rcp(V a, bool fast) {
+        return make_float2(shifted_rcp(a.x, fast), shifted_rcp(a.y, fast));
+    }
 };
 
 // density deviation, density, 1/density and momentum of shifted populations
@@ -56,7 +75,7 @@ __device__ __forceinline__ void shifted_moments(const typename L::V (&h)[S::Q], 
     for (int q = 1; q < S::Q; ++q) r = L::add(r, h[q]);
     drho = r;
     rho = L::add(r, L::set(1.0f));
-    inv = L::rcp(rho);
+    inv = L::rcp(rho, LGB_SHIFTED_FAST_RCP_2D && S::D < 3);
 #pragma unroll
     for (int d = 0; d < 3; ++d) j[d] = L::set(0.0f);
 #pragma unroll
