@@ -336,7 +336,9 @@ typedef struct {
     int32_t n_domains;
     int32_t n_tiles;
     int32_t threads;     /* threads per block (multiple of 32, <= 512) */
-    int32_t blocks;      /* resident blocks of the persistent grid */
+    int32_t blocks;      /* grid size: the blocks walk the tile table with a
+                            grid stride (as many as the SMs hold, or one
+                            block per tile) */
     const lgb_batch_domain *domains;  /* device copy of the domain table */
     const lgb_batch_tile *tiles;      /* device copy of the tile table */
     const void *f_in;    /* pool read this step */
