@@ -224,3 +224,42 @@ def test_init_and_enstrophy_validation(lgb):
     assert L.lgb_enstrophy(2, _lib.F64, ctypes.cast(bad, ctypes.c_void_p), 0x1000, 0x2000,
                            0x3000, None) != 0
     assert "must be positive" in L.lgb_last_error().decode()
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(abi_version=4), "ABI version"),
+    (dict(stencil=9), "unknown stencil"),
+    (dict(storage=9), "unknown storage"),
+    (dict(collision=3), "BGK, TRT or no collision"),
+    (dict(n_tiles=0), "empty domain or tile table"),
+    (dict(f_out=0x3000), "distinct input and output"),
+    (dict(pool_elements=0), "pool_elements must be positive"),
+    (dict(threads=48), "a multiple of 32"),
+    (dict(blocks=0), "blocks must be positive"),
+    (dict(rates=0x4004), "rates must be 16-byte aligned"),
+])
+def test_batched_step_validation_errors(lgb, kw, msg):
+    """lgb_batched_step refuses a bad descriptor before any launch"""
+    from lettuce_gb300 import _lib
+    from lettuce_gb300._batched import BatchDesc, _bind
+    L = _lib.load()
+    _bind(L)
+    d = BatchDesc()
+    d.abi_version = _lib.ABI_VERSION
+    d.stencil = _lib.D2Q9
+    d.storage = _lib.F32
+    d.collision = _lib.BGK
+    d.n_domains = 1
+    d.n_tiles = 1
+    d.threads = 128
+    d.blocks = 1
+    d.domains = 0x1000
+    d.tiles = 0x2000
+    d.f_in = 0x3000
+    d.f_out = 0x5000
+    d.pool_elements = 1024
+    for k, v in kw.items():
+        setattr(d, k, v)
+    rc = L.lgb_batched_step(ctypes.byref(d), None)
+    assert rc != 0
+    assert msg in L.lgb_last_error().decode()
