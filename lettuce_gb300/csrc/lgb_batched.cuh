@@ -1,16 +1,16 @@
 // Batched step: many periodic domains of uneven sizes advanced by one
-// persistent launch. All domains' population fields live in one pool (domain
-// b at element offset `offset`, layout [Q][N_b] as for a single grid); the
-// host cuts every domain into tiles of whole rows (lgb_batch_plan) and the
+// launch. All domains' population fields live in one pool (domain b at
+// element offset `offset`, layout [Q][N_b] as for a single grid); the host
+// cuts every domain into tiles of whole rows (lgb_batch_plan) and the
 // kernel's blocks walk the tile table with a grid stride (as many blocks as
-// the SMs hold, or one block per tile), one cell per thread, pulling from
-// the periodic neighbours inside the tile's domain.
-// The per-domain relaxation times come from the domain table. Domains of the
-// 16-bit formats whose rows are whole 32-bit words -- an even row length, or
-// an odd one stored with one pad element per row (pitch = length + 1) --
-// and whose offset is word-aligned run the two-cell step (one 32-bit word
-// per population pair, lgb_step_vec.cuh), bit-identical to the one-cell
-// step.
+// the SMs hold, or one block per tile), pulling from the periodic
+// neighbours inside the tile's domain, with the domain's relaxation times.
+// The float64 and float32 formats step one cell per thread. The 16-bit
+// formats step two cells per thread, one 32-bit word per population pair
+// (as lgb_step_vec.cuh does for a single grid): every row must be whole
+// words -- an even row length, or an odd one stored with one pad element
+// per row (pitch = length + 1) -- at an even offset; other domains are
+// flagged and skipped.
 #pragma once
 
 #include "lgb_shifted.cuh"
@@ -36,43 +36,6 @@ __device__ __forceinline__ uint32_t load_pair_padded(const uint32_t *__restrict_
     return __byte_perm(__ldg(row + tz), __ldg(row + tz + 1), 0x5432);
 }
 
-// the pull step of pair tz of row (x, y) in a domain whose rows are padded
-// to Zh words (odd row length p.Z, pitch p.Z + 1, Nh words per population
-// plane); the pad lane is computed and stored but never read by a real cell
-// and is left out of the status check
-template <int SID, int ST, int COLL>
-__device__ __forceinline__ void step_pair_padded_pull(const StepParams &p, const uint32_t tz,
-                                                      const uint32_t x, const uint32_t y,
-                                                      const uint32_t Zh, const uint32_t Nh) {
-    using S = Stencil<SID>;
-    using P = Pack16<ST>;
-    const uint32_t row = x * p.Y + y;
-    const uint32_t xm = x == 0 ? p.X - 1 : x - 1, xp = x + 1 == p.X ? 0 : x + 1;
-    const uint32_t ym = y == 0 ? p.Y - 1 : y - 1, yp = y + 1 == p.Y ? 0 : y + 1;
-    const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in);
-    auto row_of = [&](int dx, int dy) -> uint32_t {
-        const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
-        const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
-        return (a * p.Y + b) * Zh;
-    };
-    float2 h[S::Q];
-#pragma unroll
-    for (int q = 0; q < S::Q; ++q) {
-        const uint32_t *r = fin + (size_t)q * Nh + row_of(-ix<S>(q), -iy<S>(q));
-        h[q] = P::decode(load_pair_padded(r, tz, Zh, -iz<S>(q)));
-    }
-    collide_shifted<S, Lane2, COLL>(h, p.cp);
-    if (p.status) {
-        float2 r = h[0];
-#pragma unroll
-        for (int q = 1; q < S::Q; ++q) r = Lane2::add(r, h[q]);
-        if (!isfinite(r.x) || (tz + 1 < Zh && !isfinite(r.y))) atomicOr(p.status, 1u);
-    }
-    uint32_t *fout = static_cast<uint32_t *>(p.f_out);
-#pragma unroll
-    for (int q = 0; q < S::Q; ++q) fout[(size_t)q * Nh + row * Zh + tz] = P::encode(h[q]);
-}
-
 struct BatchParams {
     const void *f_in;
     void *f_out;
@@ -86,14 +49,11 @@ struct BatchParams {
 };
 
 // The 16-bit pair loop keeps its tile's domain in shared memory and reads
-// it there at every use (1), or holds it in registers (0). Kernel
-// parameters take no registers (they are read from the constant bank), a
-// tile's grid, word offset and rates do: the D2Q9 fp16 TRT kernel takes 62
-// registers in the register form, 50 in the shared-memory form, which
-// also fits the 48-register cap below without spills.
-#ifndef LGB_BATCH_LEAN
-#define LGB_BATCH_LEAN 1
-#endif
+// it there where it is used. Kernel parameters take no registers (they are
+// read from the constant bank), a tile's grid, word offset and rates do:
+// the D2Q9 fp16 TRT kernel took 62 registers with them held in registers,
+// 50 with them in shared memory, which also fits the 48-register cap below
+// without spills.
 
 // a tile of a 16-bit domain as its pair loop reads it: three 16-byte
 // groups, each read with one shared-memory load where it is used
@@ -108,11 +68,6 @@ struct alignas(16) TilePairs {
     uint32_t unused[2];
 };
 
-// The pair loop reads the tile's values as 16-byte shared-memory loads (1)
-// or field by field through a volatile reference (0).
-#ifndef LGB_BATCH_VEC_TILE
-#define LGB_BATCH_VEC_TILE 1
-#endif
 __device__ __forceinline__ uint4 lds_u4(const void *ptr) {
     uint4 v;
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(ptr);
@@ -122,80 +77,11 @@ __device__ __forceinline__ uint4 lds_u4(const void *ptr) {
 }
 
 // the pull step of the pairs t2, t2 + blockDim, ... below ts.end of a tile
-// (pair index = row Zh + word), the tile's values read from shared memory
-// where they are used; PADDED: the last word of a row holds (cell Z - 1,
-// pad), the pad lane is left out of the status check
-template <int SID, int ST, int COLL, bool PADDED>
-__device__ __forceinline__ void tile_pairs_pull(const BatchParams &p, const volatile TilePairs &ts,
-                                                uint32_t t2) {
-    using S = Stencil<SID>;
-    using P = Pack16<ST>;
-    uint32_t tz, x, y;
-    {
-        const uint32_t Zh = ts.Zh, Y = ts.Y;
-        const uint32_t row = t2 / Zh;
-        tz = t2 - row * Zh;
-        x = row / Y;
-        y = row - x * Y;
-    }
-    while (true) {
-        float2 h[S::Q];
-        {
-            const uint32_t X = ts.X, Y = ts.Y, Zh = ts.Zh, Nh = ts.Nh;
-            const uint32_t *__restrict__ fin = static_cast<const uint32_t *>(p.f_in) +
-                                               (((uint64_t)ts.word_hi << 32) | ts.word_lo);
-            const uint32_t xm = x == 0 ? X - 1 : x - 1, xp = x + 1 == X ? 0 : x + 1;
-            const uint32_t ym = y == 0 ? Y - 1 : y - 1, yp = y + 1 == Y ? 0 : y + 1;
-            const uint32_t tzm = tz == 0 ? Zh - 1 : tz - 1, tzp = tz + 1 == Zh ? 0 : tz + 1;
-#pragma unroll
-            for (int q = 0; q < S::Q; ++q) {
-                const int dx = -ix<S>(q), dy = -iy<S>(q);
-                const uint32_t a = dx == 0 ? x : (dx > 0 ? xp : xm);
-                const uint32_t b = dy == 0 ? y : (dy > 0 ? yp : ym);
-                const uint32_t *r = fin + (size_t)q * Nh + (a * Y + b) * Zh;
-                uint32_t w;
-                if constexpr (PADDED) w = load_pair_padded(r, tz, Zh, -iz<S>(q));
-                else w = load_pair(r, tz, tzm, tzp, -iz<S>(q));
-                h[q] = P::decode(w);
-            }
-        }
-        {
-            CollideParams cp;
-            cp.f_omega = ts.f_omega;
-            cp.f_one_minus_omega = ts.f_one_minus_omega;
-            cp.f_inv_2tp = ts.f_inv_2tp;
-            cp.f_inv_2tm = ts.f_inv_2tm;
-            collide_shifted<S, Lane2, COLL>(h, cp);
-        }
-        if (p.status) {
-            float2 r = h[0];
-#pragma unroll
-            for (int q = 1; q < S::Q; ++q) r = Lane2::add(r, h[q]);
-            if (!isfinite(r.x) || ((!PADDED || tz + 1 < ts.Zh) && !isfinite(r.y)))
-                atomicOr(p.status, 1u);
-        }
-        {
-            const uint32_t Nh = ts.Nh;
-            uint32_t *fout = static_cast<uint32_t *>(p.f_out) +
-                             (((uint64_t)ts.word_hi << 32) | ts.word_lo) +
-                             (x * ts.Y + y) * ts.Zh + tz;
-#pragma unroll
-            for (int q = 0; q < S::Q; ++q) fout[(size_t)q * Nh] = P::encode(h[q]);
-        }
-        t2 += blockDim.x;
-        if (t2 >= ts.end) break;
-        const uint32_t Zh = ts.Zh;
-        tz += blockDim.x;
-        while (tz >= Zh) {
-            tz -= Zh;
-            if (++y == ts.Y) { y = 0; ++x; }
-        }
-    }
-}
-
-// tile_pairs_pull reading the tile's values in 16-byte groups; the next
+// (pair index = row Zh + word), the tile's values read from shared memory in
+// 16-byte groups where they are used; PADDED: the last word of a row holds
+// (cell Z - 1, pad), the pad lane is left out of the status check. The next
 // pair lies blockDim pairs on: ts.step_rows whole rows plus blockDim mod Zh
-// words (no division, no per-row loop)
+// words (no division, no per-row loop).
 template <int SID, int ST, int COLL, bool PADDED>
 __device__ __forceinline__ void tile_pairs_pull_vec(const BatchParams &p, const TilePairs &ts,
                                                     uint32_t t2) {
@@ -339,40 +225,25 @@ __device__ __forceinline__ void setup_tile_pairs(const BatchParams &p, const int
     ts.kind = padded ? 2u : 1u;
 }
 
-// the batched step (one launch over every tile of the batch)
+// the one-cell pull step over tile t (float64 and float32 formats): every
+// thread reads and checks the tile and its domain, one thread forms the
+// rates for the block
 template <int SID, int ST, int COLL>
-__device__ __forceinline__ void batched_step_body(const BatchParams &p) {
+__device__ __forceinline__ void batched_tile_cells(const BatchParams &p, const int t,
+                                                   double (&s_rates)[3], float (&s_frates)[4]) {
     using S = Stencil<SID>;
     using Sto = Storage<ST>;
     using R = typename Sto::R;
     using T = typename Sto::T;
-    constexpr bool HSPACE = is_shifted<ST>() && shifted_collision<COLL>();
+    static_assert(!is_shifted<ST>(), "the 16-bit formats take the pair loop");
+    constexpr bool HSPACE = false;
     const T *__restrict__ pool_in = static_cast<const T *>(p.f_in);
     T *pool_out = static_cast<T *>(p.f_out);
-    __shared__ double s_rates[3];
-    __shared__ float s_frates[4];
-    __shared__ TilePairs s_pairs;
-    for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
-        if constexpr (HSPACE && LGB_BATCH_LEAN && LGB_BATCH_VEC_TILE) {
-            // the 16-bit pair loop: one thread sets the tile up (the loop
-            // bounds are uniform, so every thread reaches both barriers)
-            if (t != (int)blockIdx.x) __syncthreads();  // the previous tile is read
-            if (threadIdx.x == 0) setup_tile_pairs<SID>(p, t, s_pairs);
-            __syncthreads();
-            const uint4 bk = lds_u4(&s_pairs.begin);
-            if (bk.y != 0) {
-                const uint32_t t2 = bk.x + threadIdx.x;
-                if (t2 < lds_u4(&s_pairs.word_lo).z) {
-                    if (bk.y == 2u) tile_pairs_pull_vec<SID, ST, COLL, true>(p, s_pairs, t2);
-                    else tile_pairs_pull_vec<SID, ST, COLL, false>(p, s_pairs, t2);
-                }
-            }
-            continue;
-        }
+    {
         const lgb_batch_tile tile = p.tiles[t];
         if (tile.domain < 0 || tile.domain >= p.n_domains) {
             if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
-            continue;
+            return;
         }
         const lgb_batch_domain dom = p.domains[tile.domain];
         // the domain as an internal (X, Y, Z) grid
@@ -400,7 +271,7 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
              (uint64_t)tile.row_end <= (uint64_t)r[0] * r[1] && dom.tau > 0.0;
         if (!ok) {
             if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
-            continue;
+            return;
         }
         g.N = (uint32_t)n64;
         // the domain's relaxation rates, three float64 divisions: one thread
@@ -437,40 +308,8 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
             s_frates[1] = c.f_one_minus_omega;
             s_frates[2] = c.f_inv_2tp;
             s_frates[3] = c.f_inv_2tm;
-            if constexpr (HSPACE && LGB_BATCH_LEAN) {
-                s_pairs.f_omega = c.f_omega;
-                s_pairs.f_one_minus_omega = c.f_one_minus_omega;
-                s_pairs.f_inv_2tp = c.f_inv_2tp;
-                s_pairs.f_inv_2tm = c.f_inv_2tm;
-                const uint64_t word_offset = (uint64_t)dom.offset >> 1;
-                s_pairs.word_lo = (uint32_t)word_offset;
-                s_pairs.word_hi = (uint32_t)(word_offset >> 32);
-                s_pairs.X = r[0];
-                s_pairs.Y = r[1];
-                s_pairs.Zh = pitch >> 1;
-                s_pairs.Nh = (uint32_t)(n_alloc >> 1);
-                s_pairs.end = (uint32_t)tile.row_end * (pitch >> 1);
-                s_pairs.step_rows = blockDim.x / (pitch >> 1);
-            }
         }
         __syncthreads();
-        if constexpr (HSPACE && LGB_BATCH_LEAN) {
-            // rows of whole 32-bit words: padded odd rows, or even rows at an
-            // even offset (the others are flagged and skipped below)
-            if (padded || ((r[2] & 1u) == 0 && (dom.offset & 1) == 0)) {
-                const uint32_t t2 = (uint32_t)tile.row_begin * (pitch >> 1) + threadIdx.x;
-                if (t2 < (uint32_t)tile.row_end * (pitch >> 1)) {
-                    if constexpr (LGB_BATCH_VEC_TILE) {
-                        if (padded) tile_pairs_pull_vec<SID, ST, COLL, true>(p, s_pairs, t2);
-                        else tile_pairs_pull_vec<SID, ST, COLL, false>(p, s_pairs, t2);
-                    } else {
-                        if (padded) tile_pairs_pull<SID, ST, COLL, true>(p, s_pairs, t2);
-                        else tile_pairs_pull<SID, ST, COLL, false>(p, s_pairs, t2);
-                    }
-                }
-                continue;
-            }
-        }
         CollideParams cp;
         cp.omega = s_rates[0];
         cp.inv_2tp = s_rates[1];
@@ -486,63 +325,9 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
         // row and column are carried forward (one division per tile instead
         // of fast-division constants derived per tile)
         const uint32_t step = blockDim.x;
-        if constexpr (HSPACE) {
-            if (padded) {
-                g.f_in = fin;
-                g.f_out = fout;
-                g.cp = cp;
-                g.status = p.status;
-                const uint32_t Zh = pitch >> 1;
-                const uint32_t Nh = (uint32_t)(n_alloc >> 1);
-                const uint32_t end = (uint32_t)tile.row_end * Zh;
-                uint32_t t2 = (uint32_t)tile.row_begin * Zh + threadIdx.x;
-                if (t2 >= end) continue;
-                uint32_t row = t2 / Zh, tz = t2 - row * Zh;
-                uint32_t x = row / g.Y, y = row - x * g.Y;
-                while (true) {
-                    step_pair_padded_pull<SID, ST, COLL>(g, tz, x, y, Zh, Nh);
-                    t2 += step;
-                    if (t2 >= end) break;
-                    tz += step;
-                    while (tz >= Zh) {
-                        tz -= Zh;
-                        if (++y == g.Y) { y = 0; ++x; }
-                    }
-                }
-                continue;
-            }
-            if ((g.Z & 1u) == 0 && (dom.offset & 1) == 0) {
-                g.f_in = fin;
-                g.f_out = fout;
-                g.cp = cp;
-                g.status = p.status;
-                const uint32_t Zh = g.Z >> 1;
-                const uint32_t end = (uint32_t)tile.row_end * Zh;
-                uint32_t t2 = (uint32_t)tile.row_begin * Zh + threadIdx.x;
-                if (t2 >= end) continue;
-                uint32_t row = t2 / Zh, tz = t2 - row * Zh;
-                uint32_t x = row / g.Y, y = row - x * g.Y;
-                while (true) {
-                    step_pair_at<SID, ST, COLL, LGB_PULL>(g, tz, x, y);
-                    t2 += step;
-                    if (t2 >= end) break;
-                    tz += step;
-                    while (tz >= Zh) {
-                        tz -= Zh;
-                        if (++y == g.Y) { y = 0; ++x; }
-                    }
-                }
-                continue;
-            }
-            // rows that are not whole 32-bit words (an odd length stored
-            // without its pad, or an odd offset) have no two-cell step:
-            // flagged and skipped (the host pads every odd row)
-            if (threadIdx.x == 0 && p.status) atomicOr(p.status, 2u);
-            continue;
-        }
         const uint32_t end = (uint32_t)tile.row_end * g.Z;
         uint32_t n = (uint32_t)tile.row_begin * g.Z + threadIdx.x;
-        if (n >= end) continue;
+        if (n >= end) return;
         uint32_t row = n / g.Z, z = n - row * g.Z;
         uint32_t x = row / g.Y, y = row - x * g.Y;
         while (true) {
@@ -576,6 +361,34 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
     }
 }
 
+// the batched step (one launch over every tile of the batch)
+template <int SID, int ST, int COLL>
+__device__ __forceinline__ void batched_step_body(const BatchParams &p) {
+    constexpr bool HSPACE = is_shifted<ST>() && shifted_collision<COLL>();
+    __shared__ double s_rates[3];
+    __shared__ float s_frates[4];
+    __shared__ TilePairs s_pairs;
+    for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
+        if constexpr (HSPACE) {
+            // the 16-bit pair loop: one thread sets the tile up (the loop
+            // bounds are uniform, so every thread reaches both barriers)
+            if (t != (int)blockIdx.x) __syncthreads();  // the previous tile is read
+            if (threadIdx.x == 0) setup_tile_pairs<SID>(p, t, s_pairs);
+            __syncthreads();
+            const uint4 bk = lds_u4(&s_pairs.begin);
+            if (bk.y != 0) {
+                const uint32_t t2 = bk.x + threadIdx.x;
+                if (t2 < lds_u4(&s_pairs.word_lo).z) {
+                    if (bk.y == 2u) tile_pairs_pull_vec<SID, ST, COLL, true>(p, s_pairs, t2);
+                    else tile_pairs_pull_vec<SID, ST, COLL, false>(p, s_pairs, t2);
+                }
+            }
+        } else {
+            batched_tile_cells<SID, ST, COLL>(p, t, s_rates, s_frates);
+        }
+    }
+}
+
 // Registers. The D2Q9 / D1Q3 batches of the 16-bit formats are capped at
 // LGB_BATCH_16BIT_2D_MAXREG, those of float32 at LGB_BATCH_F32_2D_MAXREG
 // (10 and 12 resident 128-thread blocks per SM instead of 8, no spills);
@@ -588,10 +401,11 @@ __device__ __forceinline__ void batched_step_body(const BatchParams &p) {
 // 140.3k (at 44: 20 bytes of spills); with the domains' float32 rates
 // formed on the host (no float64 quotient per tile) 145.4k, and with one
 // thread setting each tile up for the block 146.7k, and with the
-// two-dimensional grids' x dropped from the pair loop 148.1k; with the next
-// pair's words
-// copied asynchronously (cp.async, 4 bytes each) into a two-stage
-// shared-memory buffer while the current pair collides, 110.8k. Float32:
+// two-dimensional grids' x dropped from the pair loop 148.1k, and with the
+// approximate reciprocal of the density (lgb_shifted.cuh) 150.9k. With the
+// next pair's words copied asynchronously (cp.async, 4 bytes each) into a
+// two-stage shared-memory buffer while the current pair collides: 110.8k.
+// Float32:
 // 76.2k uncapped (64 registers), 84.4k at 40, 82.8k at 32 (20 bytes of
 // spills); 85.0k with the host's rates.
 #ifndef LGB_BATCH_16BIT_2D_MAXREG
